@@ -1,0 +1,199 @@
+/*
+ * lesgo_gpu.h -- C ABI of the GB300-native LESGO time-step library.
+ *
+ * The library replaces the per-timestep hot path of LESGO (lesgo-jhu/lesgo):
+ * the x-y spectral derivatives, the staggered z stencils, the Lagrangian
+ * scale-dependent dynamic SGS model, the equilibrium wall model, the stress
+ * divergence, the 3/2-dealiased convective term, the FFT + tridiagonal
+ * pressure solve, the actuator-disk forcing and the AB2 advance / projection.
+ * Every field lives in GPU memory; host arrays are only touched by the
+ * explicit set/get/upload/download calls.
+ *
+ * Conventions shared with the reference:
+ *  - 3-D arrays use the reference's Fortran layout (ld, ny, lbz:nzhi),
+ *    column-major, FP64, ld = 2*(nx/2+1); the serial reference uses
+ *    lbz = 1 (p: lbz = 0) and nz = Nz+1 (param.f90:49-55,
+ *    input_util.f90:196-235).  Host <-> device copies are flat memcpys of
+ *    whole (ld, ny) planes.
+ *  - Every entry point returns an int status (LESGO_OK = 0) and never
+ *    aborts; lesgo_gpu_last_error() describes the last failure.  The
+ *    reference instead prints and stops (messages.f90:228-239,
+ *    tridag_array.f90:190-193).
+ *  - One host thread per handle; each handle owns one CUDA stream.
+ */
+#ifndef LESGO_GPU_H
+#define LESGO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  LESGO_OK = 0,
+  LESGO_ERR_ARG = 1,          /* bad argument or handle                    */
+  LESGO_ERR_CUDA = 2,         /* CUDA runtime failure                      */
+  LESGO_ERR_UNSUPPORTED = 3,  /* configuration outside the built model set */
+  LESGO_ERR_NOMEM = 4,        /* device allocation refused                 */
+  LESGO_ERR_NUMERIC = 5       /* zero pivot in the tridiagonal solve       */
+};
+
+/* ---- precision forms ---------------------------------------------------- */
+enum {
+  LESGO_FP64 = 0,   /* plain FP64 drop-in                                    */
+  LESGO_MIXED = 1   /* FP32 fields and transforms; FP64 pressure RHS,
+                       tridiagonal solve, kx=ky=0 mode and wall log law      */
+};
+
+/* ---- field identifiers (sim_param.f90:300-365, sgs_param.f90:30-184) ---- */
+enum {
+  LESGO_U = 0, LESGO_V, LESGO_W,
+  LESGO_DUDX, LESGO_DUDY, LESGO_DUDZ,
+  LESGO_DVDX, LESGO_DVDY, LESGO_DVDZ,
+  LESGO_DWDX, LESGO_DWDY, LESGO_DWDZ,
+  LESGO_RHSX, LESGO_RHSY, LESGO_RHSZ,
+  LESGO_RHSX_F, LESGO_RHSY_F, LESGO_RHSZ_F,
+  LESGO_TXX, LESGO_TXY, LESGO_TXZ, LESGO_TYY, LESGO_TYZ, LESGO_TZZ,
+  LESGO_DIVTX, LESGO_DIVTY, LESGO_DIVTZ,
+  LESGO_P, LESGO_DPDX, LESGO_DPDY, LESGO_DPDZ,
+  LESGO_FXA, LESGO_FYA, LESGO_FZA,
+  LESGO_S11, LESGO_S12, LESGO_S13, LESGO_S22, LESGO_S23, LESGO_S33,
+  LESGO_NU_T, LESGO_CS_OPT2,
+  LESGO_F_LM, LESGO_F_MM, LESGO_F_QN, LESGO_F_NN,
+  LESGO_BETA, LESGO_TN_ALL, LESGO_EE_NOW,
+  LESGO_NFIELDS
+};
+
+/* One actuator disk, lengths already divided by z_i (turbines.f90:759-785). */
+typedef struct {
+  double xloc, yloc, height, dia, thk;
+  double theta1, theta2;   /* degrees */
+  double Ct_prime;
+} lesgo_turbine_t;
+
+/* Run parameters: the subset of `param` (param.f90) and the TURBINES block
+ * that the hot path reads, as lesgo.conf gives them.  Derived sizes
+ * (nz, ld, lh, nx2, ny2, dx, dy, dz, tadv1/2, mean_p_force, delta) are
+ * computed exactly as input_util.f90:196-235, 403-409, 534-542 and
+ * sgs_param.f90:187. */
+typedef struct {
+  int nx, ny, nz_tot;              /* DOMAIN Nx, Ny, Nz                      */
+  double L_x, L_y, L_z, z_i;
+  double u_star, vonk, zo, dt;
+  int sgs_model, cs_count, dyn_init, ifilter;
+  int lbc_mom, ubc_mom;
+  int molec;
+  double nu_molec, ubot, utop;
+  int use_mean_p_force, eval_mean_p_force;
+  double mean_p_force_x, mean_p_force_y;
+  int initu;                       /* restart semantics (initial.f90:98-106) */
+  int precision;                   /* LESGO_FP64 or LESGO_MIXED              */
+  /* actuator-disk turbines (TURBINES block); n_turbines = 0 disables */
+  int n_turbines;
+  const lesgo_turbine_t* turbines;
+  double alpha1, alpha2, filter_cutoff, T_avg_dim;
+  int adm_correction;
+} lesgo_params_t;
+
+typedef struct lesgo_handle lesgo_handle_t;
+
+/* Fill *p with lesgo.conf defaults of the half-channel case (lbc_mom=2,
+ * ubc_mom=0, sgs_model=5, cs_count=5, dyn_init=100, zo=1e-4, dt=2e-4). */
+int lesgo_gpu_params_default(lesgo_params_t* p);
+
+/* Create / destroy a solver on the current CUDA device.  Replaces
+ * initialize() device-side parts: sim_param_init, sgs_param_init,
+ * init_fft, test_filter_init, grid%build, turbines_init
+ * (initialize.f90:21-202). */
+int lesgo_gpu_create(const lesgo_params_t* p, lesgo_handle_t** h);
+int lesgo_gpu_destroy(lesgo_handle_t* h);
+const char* lesgo_gpu_last_error(const lesgo_handle_t* h);
+
+/* nz (= Nz+1), ld, lh, nx2, ny2 of the handle. */
+int lesgo_gpu_dims(const lesgo_handle_t* h, int* nz, int* ld, int* lh, int* nx2, int* ny2);
+
+/* Copy planes lbz..nzhi of a Fortran (ld, ny, lbz:nzhi) FP64 host array into
+ * / out of the device field (levels outside 0..nz are rejected). */
+int lesgo_gpu_set_field(lesgo_handle_t* h, int field, const double* host, int lbz, int nzhi);
+int lesgo_gpu_get_field(lesgo_handle_t* h, int field, double* host, int lbz, int nzhi);
+
+/* Field registry: remember a Fortran module array (c_loc) for a field, then
+ * upload/download it on demand (init, checkpoint and output only). */
+int lesgo_gpu_bind_field(lesgo_handle_t* h, int field, double* host, int lbz, int nzhi);
+int lesgo_gpu_upload(lesgo_handle_t* h, int field);
+int lesgo_gpu_download(lesgo_handle_t* h, int field);
+
+/* Seeded half-channel initial condition: u = (1/0.4) ln(z/z0) (1 + 0.1 U),
+ * v, w = 0.1 U with U = U(-1,1) from a counter-based hash of
+ * (seed, field, i, j, k); w(1) = w(nz) = 0, u(nz) = u(nz-1), v(nz) = v(nz-1).
+ * Stands in for ic_les (initial.f90:550-623). */
+int lesgo_gpu_init_ic(lesgo_handle_t* h, uint64_t seed);
+
+/* ---- stage entry points (one per reference subroutine) ----------------- */
+/* derivatives.f90:166-211 */
+int lesgo_gpu_filt_da(lesgo_handle_t* h, int f, int dfdx, int dfdy);
+/* derivatives.f90:37-70, 73-106, 109-163 */
+int lesgo_gpu_ddx(lesgo_handle_t* h, int f, int dfdx);
+int lesgo_gpu_ddy(lesgo_handle_t* h, int f, int dfdy);
+int lesgo_gpu_ddxy(lesgo_handle_t* h, int f, int dfdx, int dfdy);
+/* derivatives.f90:214-264, 267-311 */
+int lesgo_gpu_ddz_uv(lesgo_handle_t* h, int f, int dfdz);
+int lesgo_gpu_ddz_w(lesgo_handle_t* h, int f, int dfdz);
+/* test_filtermodule.f90:126-147: filter plane `level` of `f` in place */
+int lesgo_gpu_test_filter(lesgo_handle_t* h, int f, int level);
+/* wallstress.f90:21-257 */
+int lesgo_gpu_wallstress(lesgo_handle_t* h);
+/* sgs_stag_util.f90:33-464 (+ lagrange_Sdep.f90, interpolag_Sdep.f90);
+ * uses the handle's step counters (jt, jt_total) */
+int lesgo_gpu_sgs_stag(lesgo_handle_t* h);
+/* divstress_uv.f90:21-85, divstress_w.f90:21-116 */
+int lesgo_gpu_divstress_uv(lesgo_handle_t* h);
+int lesgo_gpu_divstress_w(lesgo_handle_t* h);
+/* convec.f90:21-333 */
+int lesgo_gpu_convec(lesgo_handle_t* h);
+/* forcing.f90:79-117 + turbines.f90:465-638 (fxa, fya, fza) */
+int lesgo_gpu_turbines_forcing(lesgo_handle_t* h);
+/* main.f90:143-157: advance jt/jt_total and save RHS into RHS_f */
+int lesgo_gpu_begin_step(lesgo_handle_t* h);
+/* main.f90:211-267: RHS = -RHS - divt (+ mean_p_force) (+ f_a) */
+int lesgo_gpu_rhs_assemble(lesgo_handle_t* h);
+/* main.f90:273-296: Euler first step + AB2 intermediate velocity */
+int lesgo_gpu_ab2(lesgo_handle_t* h);
+/* press_stag_array.f90:21-290 with tridag_array.f90:166-246 */
+int lesgo_gpu_press_stag_array(lesgo_handle_t* h);
+/* main.f90:321-326: RHS -= grad p */
+int lesgo_gpu_rhs_sub_dp(lesgo_handle_t* h);
+/* forcing.f90:149-244 */
+int lesgo_gpu_project(lesgo_handle_t* h);
+
+/* ---- fused time loop ---------------------------------------------------- */
+/* Advance nsteps full time steps (main.f90:130-344) with fused kernels and
+ * CUDA-graph replay; identical in meaning to calling the stage entry points
+ * in the reference order. */
+int lesgo_gpu_step(lesgo_handle_t* h, int nsteps);
+/* Block until all queued work of the handle is done; reports a zero pivot
+ * met by the tridiagonal solve since the last check as LESGO_ERR_NUMERIC. */
+int lesgo_gpu_sync(lesgo_handle_t* h);
+
+/* Diagnostics as device reductions: rmsdiv (rmsdiv.f90:21-60), kinetic
+ * energy (io.f90:99-141), max CFL (cfl_util.f90:35-64) and the plane-mean
+ * bottom wall stress (functions.f90:882-905).  Any pointer may be NULL. */
+int lesgo_gpu_diag(lesgo_handle_t* h, double* rmsdiv, double* ke, double* cfl, double* tau_bot);
+
+/* Step counters (jt, jt_total) of the handle. */
+int lesgo_gpu_counters(const lesgo_handle_t* h, int* jt, int* jt_total);
+
+/* Per-turbine disk velocity u_d_T, thrust f_n and power P = -f_n u_d_T
+ * (turbines.f90:576-588) after the last turbines_forcing. */
+int lesgo_gpu_turbine_state(lesgo_handle_t* h, double* u_d_T, double* f_n, double* power, int n);
+
+/* Number of this library's kernel launches issued by one fused step of the
+ * given kind (0: normal step, 1: step with the dynamic SGS update). */
+int lesgo_gpu_launches_per_step(const lesgo_handle_t* h, int with_sgs_update);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LESGO_GPU_H */

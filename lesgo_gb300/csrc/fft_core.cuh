@@ -1,0 +1,379 @@
+// Shared-memory Stockham FFT core and the three batched plane-transform passes
+// used by every spectral stage of the LES step.
+//
+// A horizontal (x-y) transform of a stack of planes is split into
+//   Xf : real-to-complex along x (one row of nx reals per line), keeping the
+//        modes kx < nx/2 (the kx = nx/2 "oddball" is always zeroed by the
+//        reference, derivatives.f90:64, fft.f90:57-97),
+//   Y  : complex transforms along y for each kept kx column, with the
+//        stage's spectral multipliers (i kx, i ky, test-filter kernels,
+//        3/2-rule padding/truncation) applied between the forward and the
+//        inverse transform,
+//   Xi : complex-to-real along x, fused with the stage's epilogue.
+// Intermediates live in HBM as complex arrays [line][jy][kx] with kx
+// fastest, so Xf/Xi rows and Y column tiles are both coalesced.
+//
+// Transforms follow FFTW's unnormalised r2c/c2r definitions (the reference's
+// fft.f90:114-121); normalisation constants are applied by the callers
+// exactly where the reference applies them.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lesgo {
+
+template <typename R> struct CplxOf;
+template <> struct CplxOf<double> { using T = double2; };
+template <> struct CplxOf<float> { using T = float2; };
+template <typename R> using cplx = typename CplxOf<R>::T;
+
+__host__ __device__ __forceinline__ double2 mkc(double a, double b) { return make_double2(a, b); }
+__host__ __device__ __forceinline__ float2 mkc(float a, float b) { return make_float2(a, b); }
+
+template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { return mkc(a.x + b.x, a.y + b.y); }
+template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { return mkc(a.x - b.x, a.y - b.y); }
+template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+  return mkc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T2> __device__ __forceinline__ T2 cmulconj(T2 a, T2 b) {  // a * conj(b)
+  return mkc(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { return mkc(a.x, -a.y); }
+// multiply by -i (forward) or +i (inverse)
+template <typename T2> __device__ __forceinline__ T2 mul_mi(T2 a) { return mkc(a.y, -a.x); }
+template <typename T2> __device__ __forceinline__ T2 mul_pi(T2 a) { return mkc(-a.y, a.x); }
+
+constexpr int kMaxStages = 12;
+
+// Plan for one complex FFT length n = prod(radix[]).
+template <typename R>
+struct FftPlan {
+  int n;
+  int nf;
+  int radix[kMaxStages];
+  const cplx<R>* tw;   // tw[t] = exp(-2 pi i t / n), t = 0..n-1
+  const cplx<R>* rtw;  // rtw[k] = exp(-2 pi i k / (2n)), k = 0..n (real-transform packing)
+};
+
+// Radix-R butterfly on registers (DFT_R, sign by INV).
+template <typename T2, bool INV>
+__device__ __forceinline__ void bfly2(T2& a0, T2& a1) {
+  T2 t = a0;
+  a0 = cadd(t, a1);
+  a1 = csub(t, a1);
+}
+
+template <typename T2, bool INV>
+__device__ __forceinline__ void bfly4(T2& a0, T2& a1, T2& a2, T2& a3) {
+  T2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
+  T2 t2 = cadd(a1, a3), d = csub(a1, a3);
+  T2 t3 = INV ? mul_pi(d) : mul_mi(d);
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = cadd(t1, t3);
+  a3 = csub(t1, t3);
+}
+
+template <typename T2, bool INV>
+__device__ __forceinline__ void bfly3(T2& a0, T2& a1, T2& a2) {
+  using R = decltype(a0.x);
+  const R s = (R)0.86602540378443864676372317075294;  // sin(2 pi / 3)
+  T2 t1 = cadd(a1, a2);
+  T2 t2 = mkc(a0.x - (R)0.5 * t1.x, a0.y - (R)0.5 * t1.y);
+  T2 d = csub(a1, a2);
+  T2 t3 = mkc(s * d.x, s * d.y);
+  a0 = cadd(a0, t1);
+  // forward: y1 = t2 - i t3, y2 = t2 + i t3
+  T2 it3 = mul_pi(t3);
+  if (INV) {
+    a1 = cadd(t2, it3);
+    a2 = csub(t2, it3);
+  } else {
+    a1 = csub(t2, it3);
+    a2 = cadd(t2, it3);
+  }
+}
+
+template <typename T2, bool INV>
+__device__ __forceinline__ void bfly8(T2* v) {
+  using R = decltype(v[0].x);
+  const R h = (R)0.70710678118654752440084436210485;
+  // two radix-4 on even/odd, then combine with W8 twiddles
+  T2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  T2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  bfly4<T2, INV>(e0, e1, e2, e3);
+  bfly4<T2, INV>(o0, o1, o2, o3);
+  // o_k *= W8^k (forward: exp(-2 pi i k/8))
+  T2 w1 = INV ? mkc(h * (o1.x - o1.y), h * (o1.x + o1.y)) : mkc(h * (o1.x + o1.y), h * (o1.y - o1.x));
+  T2 w2 = INV ? mul_pi(o2) : mul_mi(o2);
+  T2 w3 = INV ? mkc(-h * (o3.x + o3.y), h * (o3.x - o3.y)) : mkc(h * (o3.y - o3.x), -h * (o3.x + o3.y));
+  v[0] = cadd(e0, o0);
+  v[4] = csub(e0, o0);
+  v[1] = cadd(e1, w1);
+  v[5] = csub(e1, w1);
+  v[2] = cadd(e2, w2);
+  v[6] = csub(e2, w2);
+  v[3] = cadd(e3, w3);
+  v[7] = csub(e3, w3);
+}
+
+template <typename T2, bool INV>
+__device__ __forceinline__ T2 twid(const T2* tw, int idx, T2 a) {
+  T2 w = __ldg(tw + idx);
+  return INV ? cmulconj(a, w) : cmul(a, w);
+}
+
+// Stockham autosort FFT of `nl` lines of length p.n held in shared memory
+// (line l at a + l*ls).  `b` is scratch of the same shape.  Returns the
+// buffer that holds the result.  All threads of the block must call it.
+template <typename R, bool INV>
+__device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FftPlan<R>& p) {
+  using T2 = cplx<R>;
+  const int n = p.n;
+  int Ns = 1;
+  for (int s = 0; s < p.nf; ++s) {
+    const int Rr = p.radix[s];
+    const int nb = n / Rr;
+    const int total = nl * nb;
+    const int tws = n / (Ns * Rr);
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int l = t / nb;
+      const int j = t - l * nb;
+      const int jm = j % Ns;
+      const T2* src = a + l * ls + j;
+      T2* dst = b + l * ls + (j - jm) * Rr + jm;
+      const int tb = jm * tws;
+      if (Rr == 4) {
+        T2 v0 = src[0], v1 = src[nb], v2 = src[2 * nb], v3 = src[3 * nb];
+        if (tb) {
+          v1 = twid<T2, INV>(p.tw, tb, v1);
+          v2 = twid<T2, INV>(p.tw, 2 * tb, v2);
+          v3 = twid<T2, INV>(p.tw, 3 * tb, v3);
+        }
+        bfly4<T2, INV>(v0, v1, v2, v3);
+        dst[0] = v0; dst[Ns] = v1; dst[2 * Ns] = v2; dst[3 * Ns] = v3;
+      } else if (Rr == 8) {
+        T2 v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = src[r * nb];
+        if (tb) {
+#pragma unroll
+          for (int r = 1; r < 8; ++r) v[r] = twid<T2, INV>(p.tw, r * tb, v[r]);
+        }
+        bfly8<T2, INV>(v);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) dst[r * Ns] = v[r];
+      } else if (Rr == 2) {
+        T2 v0 = src[0], v1 = src[nb];
+        if (tb) v1 = twid<T2, INV>(p.tw, tb, v1);
+        bfly2<T2, INV>(v0, v1);
+        dst[0] = v0; dst[Ns] = v1;
+      } else {  // 3
+        T2 v0 = src[0], v1 = src[nb], v2 = src[2 * nb];
+        if (tb) {
+          v1 = twid<T2, INV>(p.tw, tb, v1);
+          v2 = twid<T2, INV>(p.tw, 2 * tb, v2);
+        }
+        bfly3<T2, INV>(v0, v1, v2);
+        dst[0] = v0; dst[Ns] = v1; dst[2 * Ns] = v2;
+      }
+    }
+    __syncthreads();
+    cplx<R>* tmp = a; a = b; b = tmp;
+    Ns *= Rr;
+  }
+  return a;
+}
+
+// ---------------------------------------------------------------------------
+// Pass descriptors
+// ---------------------------------------------------------------------------
+struct XfGeom {
+  int M;        // real row length (nx or nx2)
+  int K;        // modes kept (nx/2)
+  int nrows;    // rows per field in this launch (= ny_rows * nlev)
+  int nyrows;   // rows per level (ny or ny2)
+  int rpc;      // rows per CTA
+  int ls;       // smem line stride (complex)
+  long long out_field_stride;  // complex elements between fields in the output
+};
+
+// Xf: r2c along x for NF fields at once.  Src::load2(n, jy, li, v[NF])
+// supplies the real pairs (x[2n], x[2n+1]) of every field at row (jy, li).
+// Output: out[f][li][jy][kx] for kx < K.
+template <typename R, int NF, class Src>
+__global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src, cplx<R>* __restrict__ out) {
+  using T2 = cplx<R>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* A = reinterpret_cast<T2*>(smem_raw);
+  const int nl = NF * g.rpc;
+  T2* B = A + nl * g.ls;
+  const int H = g.M / 2;
+  const int row0 = blockIdx.x * g.rpc;
+  for (int t = threadIdx.x; t < g.rpc * H; t += blockDim.x) {
+    const int r = t / H, nn = t - r * H;
+    const int row = row0 + r;
+    T2 v[NF];
+    if (row < g.nrows) {
+      const int li = row / g.nyrows;
+      const int jy = row - li * g.nyrows;
+      src.load2(nn, jy, li, v);
+    } else {
+#pragma unroll
+      for (int f = 0; f < NF; ++f) v[f] = mkc((R)0, (R)0);
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f) A[(f * g.rpc + r) * g.ls + nn] = v[f];
+  }
+  __syncthreads();
+  T2* Z = fft_lines<R, false>(A, B, nl, g.ls, plan);
+  const R half = (R)0.5;
+  for (int t = threadIdx.x; t < nl * g.K; t += blockDim.x) {
+    const int l = t / g.K, kk = t - l * g.K;
+    const int f = l / g.rpc, r = l - f * g.rpc;
+    const int row = row0 + r;
+    if (row >= g.nrows) continue;
+    T2 zk = Z[l * g.ls + kk];
+    T2 zm = Z[l * g.ls + (kk == 0 ? 0 : H - kk)];
+    T2 a = mkc(zk.x + zm.x, zk.y - zm.y);   // Zk + conj(Zm)
+    T2 b = mkc(zk.x - zm.x, zk.y + zm.y);   // Zk - conj(Zm)
+    T2 w = __ldg(plan.rtw + kk);
+    // X = a/2 - (i/2) w b
+    R wbx = w.x * b.x - w.y * b.y, wby = w.x * b.y + w.y * b.x;
+    out[(long long)f * g.out_field_stride + (long long)row * g.K + kk] = mkc(half * (a.x + wby), half * (a.y - wbx));
+  }
+}
+
+struct XiGeom {
+  int M;        // real output row length (nx or nx2)
+  int K;        // modes present in the input (nx/2); K..M/2 are zero
+  int nrows;    // rows in this launch (ny_rows * nlev)
+  int nyrows;
+  int rpc;
+  int ls;
+  long long in_field_stride;
+};
+
+// Xi: c2r along x for NF fields at once, then Dst::store(jy, li, i, vals)
+// receives the NF reconstructed reals at x index i of row (jy, li).
+template <typename R, int NF, class Dst>
+__global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const cplx<R>* __restrict__ in, Dst dst) {
+  using T2 = cplx<R>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* A = reinterpret_cast<T2*>(smem_raw);
+  const int H = g.M / 2;
+  const int nl = NF * g.rpc;
+  T2* B = A + nl * g.ls;
+  const int row0 = blockIdx.x * g.rpc;
+  // build Z[k] = (X[k] + conj X[H-k]) + i W^-k (X[k] - conj X[H-k])
+  for (int t = threadIdx.x; t < nl * H; t += blockDim.x) {
+    const int l = t / H, k = t - l * H;
+    const int f = l / g.rpc, r = l - f * g.rpc;
+    const int row = row0 + r;
+    T2 z = mkc((R)0, (R)0);
+    if (row < g.nrows) {
+      const T2* src = in + (long long)f * g.in_field_stride + (long long)row * g.K;
+      T2 xk = k < g.K ? src[k] : mkc((R)0, (R)0);
+      const int km = H - k;   // k = 0 -> Nyquist (zero)
+      T2 xm = (k > 0 && km < g.K) ? src[km] : mkc((R)0, (R)0);
+      T2 a = mkc(xk.x + xm.x, xk.y - xm.y);
+      T2 b = mkc(xk.x - xm.x, xk.y + xm.y);
+      T2 w = __ldg(plan.rtw + k);
+      R cx = w.x * b.x + w.y * b.y, cy = w.x * b.y - w.y * b.x;  // conj(w) * b
+      z = mkc(a.x - cy, a.y + cx);
+    }
+    A[l * g.ls + k] = z;
+  }
+  __syncthreads();
+  T2* Z = fft_lines<R, true>(A, B, nl, g.ls, plan);
+  const R* Zr = reinterpret_cast<const R*>(Z);
+  for (int t = threadIdx.x; t < g.rpc * g.M; t += blockDim.x) {
+    const int r = t / g.M, i = t - r * g.M;
+    const int row = row0 + r;
+    if (row >= g.nrows) continue;
+    const int li = row / g.nyrows;
+    const int jy = row - li * g.nyrows;
+    R vals[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) vals[f] = Zr[2 * ((f * g.rpc + r) * g.ls) + i];
+    dst.store(jy, li, i, vals);
+  }
+}
+
+struct YGeom {
+  int ny_in, ny_out;
+  int K;         // columns (kx < K)
+  int nlev;      // lines of planes in this launch
+  int tk;        // columns per CTA
+  int ls_in, ls_out;
+  long long in_lev_stride;   // complex elements between planes of the input
+  long long out_lev_stride;
+};
+
+// Y pass.  NIN input spectra (after Xf) are loaded per column tile and, if
+// FWD, transformed along y.  Each of NOUT outputs is a combination
+// sum_i coef(o, i, kx, ky) * F_i(ky), mapped to ny_out rows (3/2 padding or
+// truncation), inverse transformed if INV, and stored.  Op supplies
+// pointers, coefficients and the row map.
+template <typename R, int NIN, int NOUT, bool FWD, bool INV, class Op>
+__global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<R> pout, Op op) {
+  using T2 = cplx<R>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // S: NIN*tk input lines (ls_in).  X: scratch of max(NIN*tk*ls_in, 2*tk*ls_out)
+  // elements; W0/W1 (tk lines of ls_out each) alias its front.
+  T2* S = reinterpret_cast<T2*>(smem_raw);
+  T2* X = S + NIN * g.tk * g.ls_in;
+  T2* W0 = X;
+  T2* W1 = X + g.tk * g.ls_out;
+  const int kx0 = blockIdx.x * g.tk;
+  const int li = blockIdx.y;
+  const int grp = blockIdx.z;
+  const int tk = min(g.tk, g.K - kx0);
+  // load inputs: element (jy, c) of input i
+  for (int t = threadIdx.x; t < NIN * g.ny_in * g.tk; t += blockDim.x) {
+    const int c = t % g.tk;
+    const int rest = t / g.tk;
+    const int jy = rest % g.ny_in;
+    const int i = rest / g.ny_in;
+    T2 v = mkc((R)0, (R)0);
+    if (c < tk) v = op.load(grp, i, li, jy, kx0 + c);
+    S[(i * g.tk + c) * g.ls_in + jy] = v;
+  }
+  __syncthreads();
+  if (FWD) {
+    T2* res = fft_lines<R, false>(S, X, NIN * g.tk, g.ls_in, pin);
+    if (res != S) {
+      for (int t = threadIdx.x; t < NIN * g.tk * g.ls_in; t += blockDim.x) S[t] = res[t];
+      __syncthreads();
+    }
+  }
+  for (int o = 0; o < NOUT; ++o) {
+    for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
+      const int c = t / g.ny_out, ky = t - c * g.ny_out;
+      const int kx = kx0 + c;
+      T2 acc = mkc((R)0, (R)0);
+      const int kin = op.rowmap(ky);
+      if (c < tk && kin >= 0) {
+#pragma unroll
+        for (int i = 0; i < NIN; ++i) {
+          T2 cf;
+          if (op.coef(grp, o, i, kx, kin, cf)) {
+            T2 s = S[(i * g.tk + c) * g.ls_in + kin];
+            acc = cadd(acc, cmul(s, cf));
+          }
+        }
+      }
+      W0[c * g.ls_out + ky] = acc;
+    }
+    __syncthreads();
+    T2* res = W0;
+    if (INV) res = fft_lines<R, true>(W0, W1, g.tk, g.ls_out, pout);
+    for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
+      const int ky = t / g.tk, c = t - ky * g.tk;
+      if (c < tk) op.store(grp, o, li, ky, kx0 + c, res[c * g.ls_out + ky]);
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace lesgo

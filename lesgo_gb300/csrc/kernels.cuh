@@ -1,0 +1,731 @@
+// Non-spectral kernels of the LES step: the fused z-column SGS sweep, the
+// Lagrangian pathline interpolation, the batched Thomas solve, the pressure
+// correction / projection, step glue, diagnostics and the seeded IC.
+#pragma once
+#include "stages.cuh"
+
+namespace lesgo {
+
+// ---------------------------------------------------------------------------
+// Wall models (wallstress.f90:107-255), evaluated in FP64 in every form.
+// Returns txz, tyz, dudz, dvdz at the wall level.
+// ---------------------------------------------------------------------------
+struct WallOut { double txz, tyz, dudz, dvdz; };
+
+__device__ __forceinline__ WallOut wall_bottom(const KP& kp, double u1f, double v1f, double u1, double v1) {
+  WallOut o{0.0, 0.0, 0.0, 0.0};
+  if (kp.lbc == 1) {                      // ws_dns_lbc (:131-148)
+    o.dudz = (u1 - kp.ubot) / (0.5 * kp.dz);
+    o.dvdz = v1 / (0.5 * kp.dz);
+    o.txz = -kp.nu_nd * o.dudz;
+    o.tyz = -kp.nu_nd * o.dvdz;
+  } else if (kp.lbc == 2) {               // ws_equilibrium_lbc (:171-219)
+    const double denom = log(0.5 * kp.dz / kp.zo);
+    const double u_avg = sqrt(u1f * u1f + v1f * v1f);
+    const double ustar = u_avg * kp.vonk / denom;
+    const double c = -(ustar * ustar) / u_avg;
+    o.txz = c * u1f;
+    o.tyz = c * v1f;
+    o.dudz = (u1 == 0.0) ? 0.0 : ustar / (0.5 * kp.dz * kp.vonk) * u1 / u_avg;
+    o.dvdz = (v1 == 0.0) ? 0.0 : ustar / (0.5 * kp.dz * kp.vonk) * v1 / u_avg;
+  }
+  return o;
+}
+
+__device__ __forceinline__ WallOut wall_top(const KP& kp, double utf, double vtf, double ut, double vt) {
+  WallOut o{0.0, 0.0, 0.0, 0.0};
+  if (kp.ubc == 1) {                      // ws_dns_ubc (:151-168)
+    o.dudz = (kp.utop - ut) / (0.5 * kp.dz);
+    o.dvdz = -vt / (0.5 * kp.dz);
+    o.txz = -kp.nu_nd * o.dudz;
+    o.tyz = -kp.nu_nd * o.dvdz;
+  } else if (kp.ubc == 2) {               // ws_equilibrium_ubc (:222-255)
+    const double denom = log(0.5 * kp.dz / kp.zo);
+    const double u_avg = sqrt(utf * utf + vtf * vtf);
+    const double ustar = u_avg * kp.vonk / denom;
+    const double c = (ustar * ustar) / u_avg;
+    o.txz = c * utf;
+    o.tyz = c * vtf;
+    o.dudz = (ut == 0.0) ? 0.0 : -ustar / (0.5 * kp.dz * kp.vonk) * ut / u_avg;
+    o.dvdz = (vt == 0.0) ? 0.0 : -ustar / (0.5 * kp.dz * kp.vonk) * vt / u_avg;
+  }
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// Fused z-column sweep: ddz_uv/ddz_w (derivatives.f90:214-311), the wall
+// values, calc_Sij (sgs_stag_util.f90:467-634), |S|, Nu_t and the stresses
+// (sgs_stag_util.f90:223-428).  One thread owns an (i,j) column over a
+// chunk of levels [k0, k1) and recomputes the level above the chunk.
+// FLAGS: COL_DDZ compute+store dudz/dvdz/dwdz and the wall values (else
+//        they are read from their fields); COL_STORE_S store S_ij;
+//        COL_TAU emit the stresses; COL_READ_S read S_ij instead of
+//        computing them.
+// ---------------------------------------------------------------------------
+enum : int { COL_DDZ = 1, COL_STORE_S = 2, COL_TAU = 4, COL_READ_S = 8 };
+
+template <typename R>
+struct ColArgs {
+  const R *u, *v, *w, *dudx, *dudy, *dvdx, *dvdy, *dwdx, *dwdy;
+  R *dudz, *dvdz, *dwdz;
+  R *S11, *S12, *S13, *S22, *S23, *S33;
+  R *Cs, *txx, *txy, *txz, *tyy, *tyz, *tzz;
+  const R *wb_u, *wb_v, *wt_u, *wt_v;   // test-filtered wall planes
+  KP kp;
+  double delta2;
+  int chunk;
+  int cs_fill;                          // Cs_opt2 = 0.03 this step (sgs_stag_util.f90:187-189)
+};
+
+template <typename R>
+struct Sij { R s11, s12, s13, s22, s23, s33; };
+
+template <typename R, int FLAGS>
+__global__ void __launch_bounds__(256) k_column(ColArgs<R> a) {
+  const KP& kp = a.kp;
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= kp.nx * kp.ny) return;
+  const int j = col / kp.nx, i = col - j * kp.nx;
+  const int nz = kp.nz;
+  const int k0 = 1 + blockIdx.y * a.chunk;
+  if (k0 > nz) return;
+  const int k1 = min(nz + 1, k0 + a.chunk);
+  const long long P = kp.plane;
+  const long long c0 = (long long)j * kp.ld + i;
+  const R inv_dz = (R)(1.0 / kp.dz);
+  const R h = (R)0.5;
+
+  // wall values (needed at k = 1 and k = nz)
+  WallOut wb{0, 0, 0, 0}, wt{0, 0, 0, 0};
+  if (FLAGS & COL_DDZ) {
+    if (k0 == 1) {
+      double uf = 0, vf = 0;
+      if (kp.lbc == 2) { uf = a.wb_u[c0]; vf = a.wb_v[c0]; }
+      wb = wall_bottom(kp, uf, vf, (double)a.u[P + c0], (double)a.v[P + c0]);
+    }
+    if (k1 >= nz) {
+      double uf = 0, vf = 0;
+      if (kp.ubc == 2) { uf = a.wt_u[c0]; vf = a.wt_v[c0]; }
+      wt = wall_top(kp, uf, vf, (double)a.u[(nz - 1) * P + c0], (double)a.v[(nz - 1) * P + c0]);
+    }
+  }
+  auto uz_at = [&](int k) -> R {
+    const long long q = k * P + c0;
+    if (!(FLAGS & COL_DDZ)) return a.dudz[q];
+    if (k == 1) return (R)wb.dudz;
+    if (k == nz) return (R)wt.dudz;
+    return inv_dz * (a.u[q] - a.u[q - P]);
+  };
+  auto vz_at = [&](int k) -> R {
+    const long long q = k * P + c0;
+    if (!(FLAGS & COL_DDZ)) return a.dvdz[q];
+    if (k == 1) return (R)wb.dvdz;
+    if (k == nz) return (R)wt.dvdz;
+    return inv_dz * (a.v[q] - a.v[q - P]);
+  };
+  auto wz_at = [&](int k) -> R {
+    const long long q = k * P + c0;
+    if (k >= nz) return (R)0;
+    if (!(FLAGS & COL_DDZ)) return a.dwdz[q];
+    return inv_dz * (a.w[q + P] - a.w[q]);
+  };
+
+  // derivative window: values at level k-1 (p*) and k (c*)
+  R pux = 0, puy = 0, pvx = 0, pvy = 0, pwx = 0, pwy = 0, pwz = 0;
+  if (!(FLAGS & COL_READ_S) && k0 > 1) {
+    const long long q = (k0 - 1) * P + c0;
+    pux = a.dudx[q]; puy = a.dudy[q]; pvx = a.dvdx[q]; pvy = a.dvdy[q];
+    pwx = a.dwdx[q]; pwy = a.dwdy[q]; pwz = wz_at(k0 - 1);
+  }
+  Sij<R> Sp{0, 0, 0, 0, 0, 0};
+  R Np = 0;
+  const int kend = min(k1, nz);
+  for (int k = k0; k <= kend; ++k) {
+    const long long q = k * P + c0;
+    Sij<R> S;
+    if (FLAGS & COL_READ_S) {
+      S = Sij<R>{a.S11[q], a.S12[q], a.S13[q], a.S22[q], a.S23[q], a.S33[q]};
+    } else {
+      const R ux = a.dudx[q], uy = a.dudy[q], vx = a.dvdx[q], vy = a.dvdy[q];
+      const R wx = a.dwdx[q], wy = a.dwdy[q];
+      const R uz = uz_at(k), vz = vz_at(k), wz = wz_at(k);
+      if (k == 1) {
+        if (kp.lbc == 0) {
+          S = Sij<R>{ux, h * (uy + vx), h * (uz + wx), vy, h * (vz + wy), h * (wz + (R)0)};
+        } else {
+          const R wx2 = h * (wx + a.dwdx[q + P]);
+          const R wy2 = h * (wy + a.dwdy[q + P]);
+          S = Sij<R>{ux, h * (uy + vx), h * (uz + wx2), vy, h * (vz + wy2), wz};
+        }
+      } else if (k == nz) {
+        if (kp.ubc == 0) {
+          S = Sij<R>{pux, h * (puy + pvx), h * (uz + wx), pvy, h * (vz + wy), h * (pwz + (R)0)};
+        } else {
+          const R wx2 = h * (pwx + wx), wy2 = h * (pwy + wy);
+          S = Sij<R>{pux, h * (puy + pvx), h * (uz + wx2), pvy, h * (vz + wy2), pwz};
+        }
+      } else {
+        const R uyy = uy + puy, vxx = vx + pvx;
+        S = Sij<R>{h * (ux + pux), (R)0.25 * (uyy + vxx), h * (uz + wx), h * (vy + pvy), h * (vz + wy), h * (wz + pwz)};
+      }
+      if (k < k1) {
+        if (FLAGS & COL_STORE_S) {
+          a.S11[q] = S.s11; a.S12[q] = S.s12; a.S13[q] = S.s13;
+          a.S22[q] = S.s22; a.S23[q] = S.s23; a.S33[q] = S.s33;
+        }
+        if (FLAGS & COL_DDZ) {
+          a.dudz[q] = uz;
+          a.dvdz[q] = vz;
+          if (k <= nz - 1) a.dwdz[q] = wz;
+          if (k == 1) { a.txz[q] = (R)wb.txz; a.tyz[q] = (R)wb.tyz; }
+          if (k == nz) { a.txz[q] = (R)wt.txz; a.tyz[q] = (R)wt.tyz; }
+        }
+      }
+      pux = ux; puy = uy; pvx = vx; pvy = vy; pwx = wx; pwy = wy; pwz = wz;
+    }
+    if (FLAGS & COL_TAU) {
+      R cs;
+      if (a.cs_fill) {
+        cs = (R)0.03;
+        if (k < k1) a.Cs[q] = cs;
+      } else {
+        cs = a.Cs[q];
+      }
+      const R Sm = sqrt((R)2 * (S.s11 * S.s11 + S.s22 * S.s22 + S.s33 * S.s33 +
+                                (R)2 * (S.s12 * S.s12 + S.s13 * S.s13 + S.s23 * S.s23)));
+      const R Nu = Sm * cs * (R)a.delta2;
+      const int m = k - 1;   // emit the stresses of level m = k-1
+      if (m >= k0 && m <= nz - 1) {
+        const long long qm = q - P;
+        const R nu = (R)kp.nu;
+        if (m == nz - 1) {
+          if (kp.ubc == 0) {
+            const R c = h * (Np + Nu) + nu, c2 = (R)2 * (Np + nu);
+            a.txx[qm] = -c * (Sp.s11 + S.s11); a.txy[qm] = -c * (Sp.s12 + S.s12);
+            a.tyy[qm] = -c * (Sp.s22 + S.s22); a.tzz[qm] = -c * (Sp.s33 + S.s33);
+            a.txz[qm] = -c2 * Sp.s13; a.tyz[qm] = -c2 * Sp.s23;
+          } else {
+            const R c = (R)-2 * (Nu + nu), c2 = (R)-2 * (Np + nu);
+            a.txx[qm] = c * S.s11; a.txy[qm] = c * S.s12; a.tyy[qm] = c * S.s22; a.tzz[qm] = c * S.s33;
+            a.txz[qm] = c2 * Sp.s13; a.tyz[qm] = c2 * Sp.s23;
+          }
+        } else if (m == 1) {
+          if (kp.lbc == 0) {
+            const R c = h * (Np + Nu) + nu;
+            a.txx[qm] = -c * (Sp.s11 + S.s11); a.txy[qm] = -c * (Sp.s12 + S.s12);
+            a.tyy[qm] = -c * (Sp.s22 + S.s22); a.tzz[qm] = -c * (Sp.s33 + S.s33);
+          } else {
+            const R c = (R)-2 * (Np + nu);
+            a.txx[qm] = c * Sp.s11; a.txy[qm] = c * Sp.s12; a.tyy[qm] = c * Sp.s22; a.tzz[qm] = c * Sp.s33;
+          }
+        } else {
+          const R c = -h * (Np + Nu), c2 = (R)-2 * Np, c3 = (R)-2 * nu * h, c4 = (R)-2 * nu;
+          a.txx[qm] = (c + c3) * (Sp.s11 + S.s11); a.txy[qm] = (c + c3) * (Sp.s12 + S.s12);
+          a.tyy[qm] = (c + c3) * (Sp.s22 + S.s22); a.tzz[qm] = (c + c3) * (Sp.s33 + S.s33);
+          a.txz[qm] = (c2 + c4) * Sp.s13; a.tyz[qm] = (c2 + c4) * Sp.s23;
+        }
+      }
+      Np = Nu;
+    }
+    Sp = S;
+  }
+}
+
+// Plain staggered z-derivatives for the stand-alone entry points.
+// uv: dfdz(k) = (f(k)-f(k-1))/dz, k = 2..nz; w: dfdz(k) = (f(k+1)-f(k))/dz, k = 1..nz-1.
+template <typename R, bool UV>
+__global__ void k_ddz(const R* __restrict__ f, R* __restrict__ dfdz, KP kp) {
+  const long long n = (long long)kp.nx * kp.ny * kp.nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = t % kp.nx;
+    const long long r = t / kp.nx;
+    const int j = r % kp.ny;
+    const int k = 1 + (int)(r / kp.ny);
+    const long long q = k * kp.plane + (long long)j * kp.ld + i;
+    const R c = (R)(1.0 / kp.dz);
+    if (UV) { if (k >= 2) dfdz[q] = c * (f[q] - f[q - kp.plane]); }
+    else    { if (k <= kp.nz - 1) dfdz[q] = c * (f[q + kp.plane] - f[q]); }
+  }
+}
+
+// Stand-alone wallstress (wallstress.f90:21-257) from filtered planes.
+template <typename R>
+__global__ void k_wall(const R* u, const R* v, const R* wb_u, const R* wb_v, const R* wt_u, const R* wt_v,
+                       R* txz, R* tyz, R* dudz, R* dvdz, KP kp) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= kp.nx * kp.ny) return;
+  const int j = col / kp.nx, i = col - j * kp.nx;
+  const long long c0 = (long long)j * kp.ld + i;
+  const long long P = kp.plane;
+  const int nz = kp.nz;
+  WallOut b = wall_bottom(kp, kp.lbc == 2 ? (double)wb_u[c0] : 0.0, kp.lbc == 2 ? (double)wb_v[c0] : 0.0,
+                          (double)u[P + c0], (double)v[P + c0]);
+  WallOut t = wall_top(kp, kp.ubc == 2 ? (double)wt_u[c0] : 0.0, kp.ubc == 2 ? (double)wt_v[c0] : 0.0,
+                       (double)u[(nz - 1) * P + c0], (double)v[(nz - 1) * P + c0]);
+  txz[P + c0] = (R)b.txz; tyz[P + c0] = (R)b.tyz; dudz[P + c0] = (R)b.dudz; dvdz[P + c0] = (R)b.dvdz;
+  const long long qt = nz * P + c0;
+  txz[qt] = (R)t.txz; tyz[qt] = (R)t.tyz; dudz[qt] = (R)t.dudz; dvdz[qt] = (R)t.dvdz;
+}
+
+// ---------------------------------------------------------------------------
+// interpolag_Sdep.f90:21-270 with trilinear_interp_w / cell_indx_w
+// (functions.f90:188-265, 349-474): backward Lagrangian advection of the
+// four running averages.  Positions are formed in FP64.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct InterpArgs {
+  const R *u, *v, *w;
+  const R *Fin[4];
+  R* Fout[4];
+  KP kp;
+};
+
+__device__ __forceinline__ double fmodulo(double a, double p) { return a - floor(a / p) * p; }
+
+template <typename R>
+__global__ void k_interp(InterpArgs<R> a) {
+  const KP& kp = a.kp;
+  const long long n = (long long)kp.nx * kp.ny * kp.nz;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = t % kp.nx;
+  const long long r = t / kp.nx;
+  const int j = r % kp.ny;
+  const int k = 1 + (int)(r / kp.ny);
+  const long long P = kp.plane;
+  const long long q = k * P + (long long)j * kp.ld + i;
+  const int nz = kp.nz;
+  const double ldt = kp.lagran_dt, dz = kp.dz;
+  const double x = i * kp.dx, y = j * kp.dy;
+  auto zc = [&](int kk) { return (kk - 0.5) * dz; };          // grid%z
+  auto zwc = [&](int kk) { return zc(kk) - dz / 2.0; };       // grid%zw
+  double xq, yq, zq;
+  if (k == 1) {
+    xq = x - (double)a.u[q] * ldt;
+    yq = y - (double)a.v[q] * ldt;
+    zq = (kp.lbc == 0) ? zwc(1) : zc(1) - 0.25 * (double)a.w[q + P] * ldt;
+  } else if (k == nz) {
+    xq = x - (double)a.u[q - P] * ldt;
+    yq = y - (double)a.v[q - P] * ldt;
+    zq = (kp.ubc == 0) ? zwc(nz) : zc(nz - 1) - 0.25 * (double)a.w[q - P] * ldt;
+  } else {
+    xq = x - 0.5 * ((double)a.u[q - P] + (double)a.u[q]) * ldt;
+    yq = y - 0.5 * ((double)a.v[q - P] + (double)a.v[q]) * ldt;
+    zq = zwc(k) - (double)a.w[q] * ldt;
+  }
+  const double thresh = 1.0e-9;
+  double px = fmodulo(xq, kp.L_x);
+  int ist = (fabs(px) / kp.L_x < thresh) ? 1 : (fabs(px - kp.L_x) / kp.L_x < thresh) ? kp.nx : (int)floor(px / kp.dx) + 1;
+  double py = fmodulo(yq, kp.L_y);
+  int jst = (fabs(py) / kp.L_y < thresh) ? 1 : (fabs(py - kp.L_y) / kp.L_y < thresh) ? kp.ny : (int)floor(py / kp.dy) + 1;
+  ist = min(max(ist, 1), kp.nx);
+  jst = min(max(jst, 1), kp.ny);
+  const int ist1 = ist + 1 > kp.nx ? 1 : ist + 1;
+  const int jst1 = jst + 1 > kp.ny ? 1 : jst + 1;
+  const double xdiff = px - (ist - 1) * kp.dx;
+  const double ydiff = py - (jst - 1) * kp.dy;
+  int kst, kst1;
+  double zdiff;
+  if (kp.lbc > 0 && zq < zwc(2)) {
+    if (zq < zc(1)) { kst = 1; kst1 = 1; zdiff = 0.0; }
+    else { kst = 1; kst1 = 2; zdiff = 2.0 * (zq - zc(1)); }
+  } else if (kp.ubc > 0 && zq > zwc(nz - 1)) {
+    if (zq > zc(nz - 1)) { kst = nz; kst1 = nz; zdiff = 0.0; }
+    else { kst = nz - 1; kst1 = nz; zdiff = 2.0 * (zq - zwc(nz - 1)); }
+  } else {
+    if (fabs(zq - zwc(nz)) / kp.L_z < thresh) kst = nz - 1;
+    else kst = (int)floor((zq - zwc(1)) / dz) + 1;
+    // the reference assumes a Lagrangian CFL below one, which keeps kst in
+    // 1..nz-1; the clamp only guards the memory access
+    kst = min(max(kst, 1), nz - 1);
+    kst1 = kst + 1;
+    zdiff = zq - zwc(kst);
+  }
+  const long long b00 = (long long)(jst - 1) * kp.ld, b01 = (long long)(jst1 - 1) * kp.ld;
+  const int i0 = ist - 1, i1 = ist1 - 1;
+  const long long z0 = kst * P, z1 = kst1 * P;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const R* V = a.Fin[f];
+    const double v000 = V[z0 + b00 + i0], v001 = V[z0 + b00 + i1];
+    const double v010 = V[z0 + b01 + i0], v011 = V[z0 + b01 + i1];
+    const double v100 = V[z1 + b00 + i0], v101 = V[z1 + b00 + i1];
+    const double v110 = V[z1 + b01 + i0], v111 = V[z1 + b01 + i1];
+    const double u1 = v000 + xdiff * (v001 - v000) / kp.dx;
+    const double u2 = v010 + xdiff * (v011 - v010) / kp.dx;
+    const double u3 = v100 + xdiff * (v101 - v100) / kp.dx;
+    const double u4 = v110 + xdiff * (v111 - v110) / kp.dx;
+    const double u5 = u1 + ydiff * (u2 - u1) / kp.dy;
+    const double u6 = u3 + ydiff * (u4 - u3) / kp.dy;
+    a.Fout[f][q] = (R)(u5 + zdiff * (u6 - u5) / dz);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// press_stag_array.f90:186-234 + tridag_array.f90:166-246: one Thomas solve
+// per (kx, ky) column in FP64, the kx = ky = 0 mode by vertical integration,
+// Nyquist rows zeroed.  Spectra layout [level][jy][kx], kx < K.
+// ---------------------------------------------------------------------------
+struct ThomasArgs {
+  const double2 *Hx, *Hy, *Hz;   // levels 1..nz at index level-1
+  const double2 *Hb, *Ht;        // r2c of divtz(1), divtz(nz) (scaled)
+  double2* phat;                 // levels 0..nz
+  double* gam;                   // index m*P, m = 0..nz+1
+  const double *kxw, *kyw;
+  double dz;
+  int nz, ny, K;
+  int* err;
+};
+
+__global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long P = (long long)a.ny * a.K;
+  if (t >= P) return;
+  const int jy = t / a.K, kx = t - jy * a.K;
+  const int nz = a.nz, n = nz + 1;
+  const double dz = a.dz;
+  if (jy == a.ny / 2) {
+    for (int l = 0; l <= nz; ++l) a.phat[l * P + t] = make_double2(0.0, 0.0);
+    return;
+  }
+  if (kx == 0 && jy == 0) {
+    double2 p = make_double2(0.0, 0.0);
+    a.phat[t] = p;
+    const double2 hb = a.Hb[t];
+    p = make_double2(p.x - dz * hb.x, p.y - dz * hb.y);
+    a.phat[P + t] = p;
+    for (int jz = 2; jz <= nz; ++jz) {
+      const double2 hz = a.Hz[(jz - 1) * P + t];
+      p = make_double2(p.x + hz.x * dz, p.y + hz.y * dz);
+      a.phat[jz * P + t] = p;
+    }
+    return;
+  }
+  const double c3 = 1.0 / (dz * dz);
+  const double c4 = 1.0 / dz;
+  const double kxv = a.kxw[kx], kyv = a.kyw[jy];
+  const double bmid = -(kxv * kxv + kyv * kyv + 2.0 * c3);
+  // m = 1: b = -1, c = 1, r = -dz * rbottomw
+  const double2 hb = a.Hb[t];
+  double2 up = make_double2((-dz * hb.x) / -1.0, (-dz * hb.y) / -1.0);
+  a.phat[t] = up;
+  double bet = -1.0;
+  double2 hzp = a.Hz[t];   // level 1
+  for (int j = 2; j <= n; ++j) {
+    double aj, bj, r_x, r_y;
+    const double cprev = (j == 2) ? 1.0 : c3;
+    if (j <= nz) {
+      aj = c3; bj = bmid;
+      const double2 hx = a.Hx[(j - 2) * P + t], hy = a.Hy[(j - 2) * P + t];
+      const double2 hz = a.Hz[(j - 1) * P + t];
+      // i kx Hx + i ky Hy + (Hz(j) - Hz(j-1)) / dz
+      r_x = (-hx.y * kxv) + (-hy.y * kyv) + (hz.x - hzp.x) * c4;
+      r_y = (hx.x * kxv) + (hy.x * kyv) + (hz.y - hzp.y) * c4;
+      hzp = hz;
+    } else {
+      aj = -1.0; bj = 1.0;
+      const double2 ht = a.Ht[t];
+      r_x = -dz * ht.x; r_y = -dz * ht.y;
+    }
+    const double g = cprev / bet;
+    bet = bj - aj * g;
+    if (bet == 0.0) { atomicExch(a.err, 1); bet = 1.0; }
+    up = make_double2((r_x - aj * up.x) / bet, (r_y - aj * up.y) / bet);
+    a.gam[j * P + t] = g;
+    a.phat[(j - 1) * P + t] = up;
+  }
+  double2 un = up;   // u(n)
+  for (int j = n - 1; j >= 1; --j) {
+    const double g = a.gam[(j + 1) * P + t];
+    double2 uj = a.phat[(j - 1) * P + t];
+    uj = make_double2(uj.x - g * un.x, uj.y - g * un.y);
+    a.phat[(j - 1) * P + t] = uj;
+    un = uj;
+  }
+}
+
+// press_stag_array.f90:284-288 dpdz + main.f90:321-326 + forcing.f90:184-243
+// (FUSED: RHSz -= dpdz, project w, boundary conditions) or just dpdz.
+template <typename R, bool FUSED>
+__global__ void k_wproj(const R* __restrict__ p, R* dpdz, R* RHSz, R* u, R* v, R* w, KP kp) {
+  const long long n = (long long)kp.nx * kp.ny * kp.nz;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = t % kp.nx;
+  const long long r = t / kp.nx;
+  const int j = r % kp.ny;
+  const int k = 1 + (int)(r / kp.ny);
+  const long long P = kp.plane;
+  const long long q = k * P + (long long)j * kp.ld + i;
+  const R d = (p[q] - p[q - P]) / (R)kp.dz;
+  if (!FUSED) { dpdz[q] = d; return; }
+  RHSz[q] = RHSz[q] - d;
+  const int nz = kp.nz;
+  if (k >= 2 && k <= nz - 1) w[q] = w[q] + (R)kp.dt * (-(R)kp.tadv1 * d);
+  if (k == 1) w[q] = (R)0;
+  if (k == nz) {
+    w[q] = (R)0;
+    if (kp.ubc == 0) { u[q] = u[q - P]; v[q] = v[q - P]; }
+  }
+}
+
+// forcing.f90:149-244 stand-alone projection (two kernels: update, then BCs).
+template <typename R>
+__global__ void k_project(const R* dpdx, const R* dpdy, const R* dpdz, R* u, R* v, R* w, KP kp) {
+  const long long n = (long long)kp.nx * kp.ny * kp.nz;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = t % kp.nx;
+  const long long r = t / kp.nx;
+  const int j = r % kp.ny;
+  const int k = 1 + (int)(r / kp.ny);
+  const long long q = k * kp.plane + (long long)j * kp.ld + i;
+  const R dt = (R)kp.dt, t1 = (R)kp.tadv1;
+  if (k <= kp.nz - 1) {
+    u[q] = u[q] + dt * (-t1 * dpdx[q]);
+    v[q] = v[q] + dt * (-t1 * dpdy[q]);
+  }
+  if (k >= 2 && k <= kp.nz - 1) w[q] = w[q] + dt * (-t1 * dpdz[q]);
+}
+
+template <typename R>
+__global__ void k_project_bc(R* u, R* v, R* w, KP kp) {
+  const long long pl = kp.plane;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= pl) return;
+  const int nz = kp.nz;
+  if (kp.ubc == 0) { u[nz * pl + t] = u[(nz - 1) * pl + t]; v[nz * pl + t] = v[(nz - 1) * pl + t]; }
+  w[nz * pl + t] = (R)0;
+  w[pl + t] = (R)0;
+}
+
+// main.f90 step glue for the stand-alone entry points (whole planes, like
+// the reference's array syntax).
+template <typename R>
+__global__ void k_rhs_assemble(R* RHSx, R* RHSy, R* RHSz, const R* divtx, const R* divty, const R* divtz,
+                               const R* fxa, const R* fya, const R* fza, KP kp) {
+  const long long pl = kp.plane;
+  const long long n = pl * kp.nz;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const long long q = pl + t;   // levels 1..nz
+  const int k = 1 + (int)(t / pl);
+  if (k <= kp.nz - 1) {
+    R x = -RHSx[q] - divtx[q], y = -RHSy[q] - divty[q], z = -RHSz[q] - divtz[q];
+    if (kp.use_mpf) { x = x + (R)kp.mpfx; y = y + (R)kp.mpfy; }
+    if (kp.turbines) { x = x + fxa[q]; y = y + fya[q]; z = z + fza[q]; }
+    RHSx[q] = x; RHSy[q] = y; RHSz[q] = z;
+  } else {
+    RHSz[q] = -RHSz[q] - divtz[q];
+  }
+}
+
+template <typename R>
+__global__ void k_ab2(R* u, R* v, R* w, const R* RHSx, const R* RHSy, const R* RHSz,
+                      const R* fx, const R* fy, const R* fz, KP kp) {
+  const long long pl = kp.plane;
+  const long long n = pl * kp.nz;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const long long q = pl + t;
+  const int k = 1 + (int)(t / pl);
+  const R dt = (R)kp.dt, t1 = (R)kp.tadv1, t2 = (R)kp.tadv2;
+  if (k <= kp.nz - 1) {
+    u[q] = u[q] + dt * (t1 * RHSx[q] + t2 * fx[q]);
+    v[q] = v[q] + dt * (t1 * RHSy[q] + t2 * fy[q]);
+  }
+  w[q] = w[q] + dt * (t1 * RHSz[q] + t2 * fz[q]);
+}
+
+template <typename R>
+__global__ void k_rhs_sub_dp(R* RHSx, R* RHSy, R* RHSz, const R* dpdx, const R* dpdy, const R* dpdz, KP kp) {
+  const long long pl = kp.plane;
+  const long long n = pl * kp.nz;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const long long q = pl + t;
+  const int k = 1 + (int)(t / pl);
+  if (k <= kp.nz - 1) { RHSx[q] = RHSx[q] - dpdx[q]; RHSy[q] = RHSy[q] - dpdy[q]; }
+  RHSz[q] = RHSz[q] - dpdz[q];
+}
+
+template <typename R>
+__global__ void k_fill(R* p, long long n, R val) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) p[t] = val;
+}
+
+template <typename A, typename B>
+__global__ void k_convert(const A* __restrict__ src, B* __restrict__ dst, long long n) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = (B)src[t];
+}
+
+// ---------------------------------------------------------------------------
+// Seeded IC: counter-based splitmix64 hash of (seed, field, i, j, k).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double hash_pm1(uint64_t seed, uint64_t fld, uint64_t i, uint64_t j, uint64_t k) {
+  uint64_t key = seed * 8ull + fld;
+  key = key * 65536ull + k;
+  key = key * 65536ull + j;
+  key = key * 65536ull + i;
+  uint64_t x = key + 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  x = x ^ (x >> 31);
+  const double u01 = (double)(x >> 11) * (1.0 / 9007199254740992.0);
+  return 2.0 * u01 - 1.0;
+}
+
+template <typename R>
+__global__ void k_ic(R* u, R* v, R* w, KP kp, uint64_t seed) {
+  const long long pl = kp.plane;
+  const long long n = pl * (kp.nz + 1);
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int k = (int)(t / pl);
+  const long long rr = t - (long long)k * pl;
+  const int j = (int)(rr / kp.ld), i = (int)(rr - (long long)j * kp.ld);
+  const int nz = kp.nz;
+  double uu = 0, vv = 0, ww = 0;
+  const int kk = (k == nz) ? nz - 1 : k;   // u(nz) = u(nz-1), v(nz) = v(nz-1)
+  if (i < kp.nx && kk >= 1 && kk <= nz - 1) {
+    const double zk = (kk - 0.5) * kp.dz;
+    const double ubar = (1.0 / 0.4) * log(zk / kp.zo);
+    uu = ubar * (1.0 + 0.1 * hash_pm1(seed, 0, i, j, kk));
+    vv = 0.1 * hash_pm1(seed, 1, i, j, kk);
+    if (k >= 2 && k <= nz - 1) ww = 0.1 * hash_pm1(seed, 2, i, j, k);
+  }
+  u[t] = (R)uu; v[t] = (R)vv; w[t] = (R)ww;
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics: per-block partial sums / maxima, then one reduction block.
+// slots: 0 sum|div|, 1 sum ke, 2 max|u|, 3 max|v|, 4 max|w|, 5 sum txz(1), 6 sum tyz(1)
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) k_diag(const R* dudx, const R* dvdy, const R* dwdz, const R* u, const R* v,
+                                              const R* w, const R* txz, const R* tyz, KP kp, double* partial) {
+  __shared__ double sh[7][256];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  const long long n = (long long)kp.nx * kp.ny * (kp.nz - 1);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = t % kp.nx;
+    const long long r = t / kp.nx;
+    const int j = r % kp.ny;
+    const int k = 1 + (int)(r / kp.ny);
+    const long long q = k * kp.plane + (long long)j * kp.ld + i;
+    acc[0] += fabs((double)dudx[q] + (double)dvdy[q] + (double)dwdz[q]);
+    const double tw = 0.5 * ((double)w[q] + (double)w[q + kp.plane]);
+    acc[1] += (double)u[q] * u[q] + (double)v[q] * v[q] + tw * tw;
+    acc[2] = fmax(acc[2], fabs((double)u[q]));
+    acc[3] = fmax(acc[3], fabs((double)v[q]));
+    acc[4] = fmax(acc[4], fabs((double)w[q]));
+    if (k == 1) { acc[5] += (double)txz[q]; acc[6] += (double)tyz[q]; }
+  }
+  for (int s = 0; s < 7; ++s) sh[s][threadIdx.x] = acc[s];
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      for (int s = 0; s < 7; ++s) {
+        if (s >= 2 && s <= 4) sh[s][threadIdx.x] = fmax(sh[s][threadIdx.x], sh[s][threadIdx.x + st]);
+        else sh[s][threadIdx.x] += sh[s][threadIdx.x + st];
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 7) partial[blockIdx.x * 7 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_diag_final(const double* partial, int nblocks, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < nblocks; ++b)
+    for (int s = 0; s < 7; ++s) {
+      const double x = partial[b * 7 + s];
+      if (s >= 2 && s <= 4) acc[s] = fmax(acc[s], x); else acc[s] += x;
+    }
+  for (int s = 0; s < 7; ++s) out[s] = acc[s];
+}
+
+// ---------------------------------------------------------------------------
+// Actuator disks (turbines.f90:465-638).  Node lists are static; the
+// reduction is one block per turbine, the scatter writes each node once with
+// the value of the last turbine that claims it (the reference assigns in
+// turbine order, turbines.f90:601-616).
+// ---------------------------------------------------------------------------
+struct TurbDev {
+  int nturb;
+  const int* node_off;      // [nturb+1] into node arrays
+  const long long* node_q;  // flat index (level, jy, i) of each node
+  const double* node_ind;   // indicator value
+  const int* win_turb;      // scatter list: turbine owning node (last writer)
+  const long long* win_q;
+  const double* win_ind;
+  int nwin;
+  const double* nhat;       // [nturb*3]
+  const double* ctp;        // Ct'
+  const double* corr;       // 1 + 0.25 (1-M) Ct' or 1
+  double* u_d;              // state
+  double* u_d_T;
+  double* f_n;
+  double* disk;             // scratch per turbine
+  double eps, dvol;
+  const double* dia;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_turb_disk(TurbDev td, const R* u, const R* v, const R* w, long long plane, int nz) {
+  __shared__ double sh[256];
+  const int s = blockIdx.x;
+  double acc = 0.0;
+  const double n0 = td.nhat[3 * s], n1 = td.nhat[3 * s + 1], n2 = td.nhat[3 * s + 2];
+  for (int l = td.node_off[s] + threadIdx.x; l < td.node_off[s + 1]; l += blockDim.x) {
+    const long long q = td.node_q[l];
+    // interp_to_uv_grid (functions.f90:87-105): level nz repeats level nz-1
+    const long long qq = (q / plane >= nz) ? q - plane : q;
+    const double wuv = 0.5 * ((double)w[qq + plane] + (double)w[qq]);
+    acc += td.dvol * td.node_ind[l] * (n0 * (double)u[q] + n1 * (double)v[q] + n2 * wuv);
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double ud = sh[0];
+    ud = ud / td.corr[s];
+    const double udT = (1.0 - td.eps) * td.u_d_T[s] + td.eps * ud;
+    td.u_d[s] = ud;
+    td.u_d_T[s] = udT;
+    // turbines.f90:583: -0.5*Ct'*abs(u_d_T)*u_d_T*0.25*pi*dia**2
+    td.f_n[s] = -0.5 * td.ctp[s] * fabs(udT) * udT * 0.25 * 3.14159265358979323846 * (td.dia[s] * td.dia[s]);
+  }
+}
+
+template <typename R>
+__global__ void k_turb_scatter(TurbDev td, R* fxa, R* fya, R* fza) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= td.nwin) return;
+  const int s = td.win_turb[l];
+  const double fn = td.f_n[s], ind = td.win_ind[l];
+  const long long q = td.win_q[l];
+  fxa[q] = (R)(fn * td.nhat[3 * s] * ind);
+  fya[q] = (R)(fn * td.nhat[3 * s + 1] * ind);
+  fza[q] = (R)(fn * td.nhat[3 * s + 2] * ind);
+}
+
+// fza onto the w grid (functions.f90:131-185): fzw(k) = (fza(k-1)+fza(k))/2,
+// k >= 2, fzw(1) = 0, over the turbine footprint columns.
+template <typename R>
+__global__ void k_turb_fzw(const R* fza, R* fzw, const long long* cols, int ncols, KP kp) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)ncols * kp.nz) return;
+  const int c = t % ncols;
+  const int k = 1 + (int)(t / ncols);
+  const long long q = k * kp.plane + cols[c];
+  fzw[q] = (k == 1) ? (R)0 : (R)0.5 * (fza[q - kp.plane] + fza[q]);
+}
+
+}  // namespace lesgo

@@ -1,0 +1,1274 @@
+// Host orchestration of the GB300 LES step and the C ABI declared in
+// include/lesgo_gpu.h.  One Solver<R> per handle owns the device field
+// store, the FFT tables, the scratch spectra, one CUDA stream and the
+// captured CUDA graphs of the steady steps.
+#include "lesgo_gpu.h"
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace lesgo {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(x)                                                                                 \
+  do {                                                                                        \
+    cudaError_t e_ = (x);                                                                     \
+    if (e_ != cudaSuccess)                                                                    \
+      throw Error(e_ == cudaErrorMemoryAllocation ? LESGO_ERR_NOMEM : LESGO_ERR_CUDA,         \
+                  std::string(#x) + ": " + cudaGetErrorString(e_));                           \
+  } while (0)
+
+static const long double kPiL = 3.141592653589793238462643383279502884L;
+static const double kPi = 3.1415926535897932384626433;   // param.f90:94
+
+// Radix schedule for a 2^a 3^b length: radix-8 stages, then 4s, at most one 2, then 3s.
+static std::vector<int> factorize(int n) {
+  int m = n, e2 = 0, e3 = 0;
+  while (m % 2 == 0) { m /= 2; ++e2; }
+  while (m % 3 == 0) { m /= 3; ++e3; }
+  if (m != 1 || n < 1) throw Error(LESGO_ERR_UNSUPPORTED, "transform length " + std::to_string(n) + " is not 2^a 3^b");
+  std::vector<int> r;
+  if (e2 % 3 == 0) { for (int i = 0; i < e2 / 3; ++i) r.push_back(8); }
+  else if (e2 % 3 == 1) {
+    if (e2 >= 4) { for (int i = 0; i < (e2 - 4) / 3; ++i) r.push_back(8); r.push_back(4); r.push_back(4); }
+    else r.push_back(2);
+  } else { for (int i = 0; i < (e2 - 2) / 3; ++i) r.push_back(8); r.push_back(4); }
+  for (int i = 0; i < e3; ++i) r.push_back(3);
+  if ((int)r.size() > kMaxStages) throw Error(LESGO_ERR_UNSUPPORTED, "too many radix stages");
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Derived run parameters (input_util.f90:196-235, 403-409, 534-542; sgs_param.f90:187)
+// ---------------------------------------------------------------------------
+struct Derived {
+  lesgo_params_t p;
+  int nx, ny, nz, nz_tot, ld, lh, nx2, ny2, ld_big, K;
+  double dx, dy, dz, tadv1, tadv2, mpfx, mpfy, delta, nu, lagran_dt;
+  std::vector<lesgo_turbine_t> turbines;
+
+  explicit Derived(const lesgo_params_t& in) : p(in) {
+    if (p.nx < 4 || p.ny < 2 || p.nz_tot < 3) throw Error(LESGO_ERR_ARG, "grid too small");
+    if (p.nx % 4 != 0 || p.ny % 2 != 0) throw Error(LESGO_ERR_UNSUPPORTED, "nx must be a multiple of 4 and ny even");
+    if (p.sgs_model != 5) throw Error(LESGO_ERR_UNSUPPORTED, "only sgs_model = 5 (Lagrangian scale-dependent)");
+    if (p.ifilter != 1) throw Error(LESGO_ERR_UNSUPPORTED, "only ifilter = 1 (spectral cut-off)");
+    if (p.lbc_mom < 0 || p.lbc_mom > 2 || p.ubc_mom < 0 || p.ubc_mom > 2)
+      throw Error(LESGO_ERR_UNSUPPORTED, "lbc_mom / ubc_mom must be 0, 1 or 2");
+    if (p.cs_count < 1) throw Error(LESGO_ERR_ARG, "cs_count must be >= 1");
+    if (p.precision != LESGO_FP64 && p.precision != LESGO_MIXED) throw Error(LESGO_ERR_ARG, "precision");
+    if (p.dt <= 0 || p.L_x <= 0 || p.L_y <= 0 || p.L_z <= 0 || p.zo <= 0) throw Error(LESGO_ERR_ARG, "non-positive length/time");
+    nx = p.nx; ny = p.ny;
+    const int nproc = 1;
+    nz = p.nz_tot / nproc + 1;
+    nz_tot = (nz - 1) * nproc + 1;
+    nx2 = 3 * nx / 2; ny2 = 3 * ny / 2;
+    lh = nx / 2 + 1; ld = 2 * lh;
+    ld_big = 2 * (nx2 / 2 + 1);
+    K = nx / 2;
+    dx = p.L_x / nx;
+    dy = p.L_y / ny;
+    dz = p.L_z / (nz_tot - 1);
+    tadv1 = 1.5; tadv2 = 1.0 - tadv1;
+    mpfx = p.mean_p_force_x; mpfy = p.mean_p_force_y;
+    if (p.use_mean_p_force && p.eval_mean_p_force) {
+      mpfx = mpfx / std::sqrt(mpfx * mpfx + mpfy * mpfy) / p.L_z;
+      mpfy = mpfy / std::sqrt(mpfx * mpfx + mpfy * mpfy) / p.L_z;
+    }
+    delta = 1.0 * std::pow(dx * dy * dz, 1.0 / 3.0);
+    nu = p.molec ? p.nu_molec / (p.u_star * p.z_i) : 0.0;
+    lagran_dt = (double)p.cs_count * p.dt;
+    if (p.n_turbines > 0) {
+      if (!p.turbines) throw Error(LESGO_ERR_ARG, "turbines == NULL");
+      turbines.assign(p.turbines, p.turbines + p.n_turbines);
+    }
+    this->p.turbines = nullptr;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Actuator-disk indicator (turbine_indicator.f90:43-169) and node search
+// (turbines.f90:123-462), computed once on the host.
+// ---------------------------------------------------------------------------
+static void fft_inplace(std::complex<double>* a, int n, int stride, bool inv,
+                        const std::vector<std::complex<double>>& tw) {
+  // iterative radix-2 (n a power of two); tw[t] = exp(-2 pi i t / n)
+  for (int i = 1, j = 0; i < n; ++i) {
+    int bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap(a[(long long)i * stride], a[(long long)j * stride]);
+  }
+  for (int len = 2; len <= n; len <<= 1) {
+    const int step = n / len;
+    for (int i = 0; i < n; i += len)
+      for (int k = 0; k < len / 2; ++k) {
+        std::complex<double> w = tw[k * step];
+        if (inv) w = std::conj(w);
+        std::complex<double>& x = a[(long long)(i + k) * stride];
+        std::complex<double>& y = a[(long long)(i + k + len / 2) * stride];
+        const std::complex<double> t = y * w;
+        y = x - t;
+        x = x + t;
+      }
+  }
+}
+
+struct Indicator {
+  std::vector<double> r, R2;
+  double ell, thk, s6d1, M;
+  double val(double rd, double x) const {
+    const double rr = rd / ell, xx = x / ell;
+    // linear_interp (functions.f90:712-735): clamp outside the table
+    double R;
+    const int N = (int)r.size();
+    int i = (int)(std::upper_bound(r.begin(), r.end(), rr) - r.begin());  // r[i-1] <= rr < r[i]
+    if (i == 0) R = R2[0];
+    else if (i >= N) R = R2[N - 1];
+    else R = R2[i - 1] + (rr - r[i - 1]) * (R2[i] - R2[i - 1]) / (r[i] - r[i - 1]);
+    const double R1 = 0.5 / thk * (std::erf(s6d1 * (xx + 0.5 * thk)) - std::erf(s6d1 * (xx - 0.5 * thk)));
+    return R1 * R / (ell * ell * ell);
+  }
+};
+
+static Indicator make_indicator(double delta1, double delta2, double thk, double dia) {
+  const int N = 2048;
+  Indicator ind;
+  ind.ell = 0.5 * dia;
+  const double d1 = delta1 / ind.ell, d2 = delta2 / ind.ell;
+  ind.thk = thk / ind.ell;
+  ind.s6d1 = std::sqrt(6.0) / d1;
+  const double L = 1 + 10 * d2 / std::sqrt(12.0);
+  const double d = 2 * L / N;
+  std::vector<double> yz(N);
+  for (int i = 0; i < N; ++i) yz[i] = -L + d * ((i + 1) - 0.5);
+  std::vector<std::complex<double>> g((size_t)N * N), h((size_t)N * N);
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i) {
+      const double r2 = yz[i] * yz[i] + yz[j] * yz[j];
+      g[(size_t)j * N + i] = 6.0 / (kPi * d2 * d2) * std::exp(-6 * r2 / (d2 * d2));
+      h[(size_t)j * N + i] = (std::sqrt(r2) < 1) ? 1.0 / kPi : 0.0;
+    }
+  std::vector<std::complex<double>> tw(N);
+  for (int t = 0; t < N; ++t) {
+    const long double a = -2.0L * kPiL * t / N;
+    tw[t] = std::complex<double>((double)cosl(a), (double)sinl(a));
+  }
+  for (auto* A : {&g, &h}) {
+    for (int j = 0; j < N; ++j) fft_inplace(A->data() + (size_t)j * N, N, 1, false, tw);
+    for (int i = 0; i < N; ++i) fft_inplace(A->data() + i, N, N, false, tw);
+  }
+  for (size_t t = 0; t < g.size(); ++t) g[t] = g[t] * h[t] * (d * d);
+  for (int i = 0; i < N; ++i) fft_inplace(g.data() + i, N, N, true, tw);
+  for (int j = 0; j < N; ++j) fft_inplace(g.data() + (size_t)j * N, N, 1, true, tw);
+  // FFTW c2r is unnormalised: fx = N^2 (g*h d^2); R2 = fx(1, 1:N/2) / N^2
+  ind.r.resize(N / 2);
+  ind.R2.resize(N / 2);
+  for (int jj = 0; jj < N / 2; ++jj) {
+    ind.r[jj] = yz[jj] + L;
+    ind.R2[jj] = g[(size_t)jj * N + 0].real() / ((double)N * N);
+  }
+  const double dr = ind.r[1] - ind.r[0];
+  double s = 0;
+  for (int jj = 0; jj < N / 2; ++jj) s += 2 * kPi * ind.r[jj] * ind.R2[jj] * dr;
+  for (auto& x : ind.R2) x /= s;
+  double m = 0;
+  for (int jj = 0; jj < N / 2; ++jj) m += 2 * kPi * ind.r[jj] * ind.R2[jj] * ind.R2[jj] * dr;
+  ind.M = m * kPi;
+  return ind;
+}
+
+static long long nint_f(double x) { return x >= 0 ? (long long)std::floor(x + 0.5) : -(long long)std::floor(-x + 0.5); }
+
+struct TurbineHost {
+  int n = 0;
+  std::vector<int> node_off;
+  std::vector<long long> node_q;
+  std::vector<double> node_ind;
+  std::vector<int> win_turb;
+  std::vector<long long> win_q;
+  std::vector<double> win_ind;
+  std::vector<long long> cols;    // (jy*ld + i) of footprint columns
+  std::vector<double> nhat, ctp, corr, dia;
+};
+
+static TurbineHost turbines_init_host(const Derived& d) {
+  TurbineHost th;
+  th.n = (int)d.turbines.size();
+  if (th.n == 0) return th;
+  const auto& P = d.p;
+  std::vector<lesgo_turbine_t> ts = d.turbines;
+  const double dx = d.dx, dy = d.dy, dz = d.dz;
+  for (auto& t : ts) t.thk = std::max(t.thk, dx * (double)1.01f);   // turbines.f90:180 (single-precision literal)
+  const double diag = std::sqrt(dx * dx + dy * dy + dz * dz);
+  const double delta1 = P.alpha1 * diag, delta2 = P.alpha2 * diag;
+  std::map<std::pair<double, double>, Indicator> cache;
+  const long long plane = (long long)d.ld * d.ny;
+  th.node_off.push_back(0);
+  for (int s = 0; s < th.n; ++s) {
+    const auto& t = ts[s];
+    auto key = std::make_pair(t.thk, t.dia);
+    if (!cache.count(key)) cache[key] = make_indicator(delta1, delta2, t.thk, t.dia);
+    const Indicator& ind = cache[key];
+    const double search_rad = 0.5 * t.dia + 3 * std::max(P.alpha1, P.alpha2) * diag;
+    const int imax = std::min((int)(search_rad / dx + 2), d.nx / 2);
+    const int jmax = std::min((int)(search_rad / dy + 2), d.ny / 2);
+    const double n1 = -std::cos(kPi * t.theta1 / 180.) * std::cos(kPi * t.theta2 / 180.);
+    const double n2 = -std::sin(kPi * t.theta1 / 180.) * std::cos(kPi * t.theta2 / 180.);
+    const double n3 = std::sin(kPi * t.theta2 / 180.);
+    const long long icp = nint_f(t.xloc / dx), jcp = nint_f(t.yloc / dy);
+    const double filt_max = ind.val(0.0, 0.0);
+    double sumA = 0.0;
+    std::vector<long long> q;
+    std::vector<double> fv;
+    for (int k = 1; k <= d.nz; ++k) {
+      if (k > d.nz_tot) continue;
+      const double zt = (k - 0.5) * dz;
+      for (long long j = jcp - jmax + 1; j <= jcp + jmax; ++j)
+        for (long long i = icp - imax + 1; i <= icp + imax; ++i) {
+          long long i2 = i, j2 = j;
+          double rx, ry;
+          if (i < 1) { i2 = ((i + d.nx - 1) % d.nx) + 1; rx = ((i2 - 1) * dx - P.L_x) - t.xloc; }
+          else if (i > d.nx) { i2 = ((i + d.nx - 1) % d.nx) + 1; rx = (P.L_x + (i2 - 1) * dx) - t.xloc; }
+          else rx = (i - 1) * dx - t.xloc;
+          if (j < 1) { j2 = ((j + d.ny - 1) % d.ny) + 1; ry = ((j2 - 1) * dy - P.L_y) - t.yloc; }
+          else if (j > d.ny) { j2 = ((j + d.ny - 1) % d.ny) + 1; ry = (P.L_y + (j2 - 1) * dy) - t.yloc; }
+          else ry = (j - 1) * dy - t.yloc;
+          const double rz = zt - t.height;
+          const double r = std::sqrt(rx * rx + ry * ry + rz * rz);
+          const double r_norm = std::fabs(rx * n1 + ry * n2 + rz * n3);
+          const double r_disk = std::sqrt(r * r - r_norm * r_norm);
+          const double filt = ind.val(r_disk, r_norm);
+          if (filt > P.filter_cutoff * filt_max) {
+            q.push_back((long long)k * plane + (j2 - 1) * d.ld + (i2 - 1));
+            fv.push_back(filt);
+            sumA += filt * dx * dy * dz;
+          }
+        }
+    }
+    for (size_t l = 0; l < q.size(); ++l) {
+      th.node_q.push_back(q[l]);
+      th.node_ind.push_back(fv[l] / sumA);
+    }
+    th.node_off.push_back((int)th.node_q.size());
+    th.nhat.insert(th.nhat.end(), {n1, n2, n3});
+    th.ctp.push_back(t.Ct_prime);
+    th.corr.push_back(P.adm_correction ? (1 + 0.25 * (1 - ind.M) * t.Ct_prime) : 1.0);
+    th.dia.push_back(t.dia);
+  }
+  // scatter list: the last turbine in order owns a shared node
+  std::unordered_map<long long, std::pair<int, double>> owner;
+  std::vector<long long> order;
+  for (int s = 0; s < th.n; ++s)
+    for (int l = th.node_off[s]; l < th.node_off[s + 1]; ++l) {
+      if (!owner.count(th.node_q[l])) order.push_back(th.node_q[l]);
+      owner[th.node_q[l]] = {s, th.node_ind[l]};
+    }
+  std::unordered_map<long long, int> colset;
+  for (long long q : order) {
+    th.win_q.push_back(q);
+    th.win_turb.push_back(owner[q].first);
+    th.win_ind.push_back(owner[q].second);
+    const long long c = q % plane;
+    if (!colset.count(c)) { colset[c] = 1; th.cols.push_back(c); }
+  }
+  return th;
+}
+
+// ---------------------------------------------------------------------------
+// Solver
+// ---------------------------------------------------------------------------
+class SolverBase {
+ public:
+  virtual ~SolverBase() {}
+  virtual const Derived& der() const = 0;
+  virtual void set_field(int f, const double* h, int lbz, int nzhi) = 0;
+  virtual void get_field(int f, double* h, int lbz, int nzhi) = 0;
+  virtual void init_ic(uint64_t seed) = 0;
+  virtual void filt_da(int f, int dx, int dy) = 0;
+  virtual void ddxy(int f, int dx, int dy) = 0;   // dx or dy may be -1
+  virtual void ddz(int f, int dfdz, bool uv) = 0;
+  virtual void test_filter(int f, int level) = 0;
+  virtual void wallstress() = 0;
+  virtual void sgs_stag() = 0;
+  virtual void divstress(int which) = 0;
+  virtual void convec() = 0;
+  virtual void turbines_forcing() = 0;
+  virtual void begin_step() = 0;
+  virtual void rhs_assemble() = 0;
+  virtual void ab2() = 0;
+  virtual void press_stag_array() = 0;
+  virtual void rhs_sub_dp() = 0;
+  virtual void project() = 0;
+  virtual void step(int n) = 0;
+  virtual int sync() = 0;
+  virtual void diag(double* out4) = 0;
+  virtual void counters(int* jt, int* jt_total) const = 0;
+  virtual void turbine_state(double* udT, double* fn, double* pw, int n) = 0;
+  virtual int launches_per_step(int with_sgs) const = 0;
+};
+
+template <typename R>
+class Solver : public SolverBase {
+  using T2 = cplx<R>;
+
+ public:
+  explicit Solver(const Derived& d) : d_(d) {
+    CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    const int nx = d_.nx, ny = d_.ny, nz = d_.nz;
+    kp_.nx = nx; kp_.ny = ny; kp_.nz = nz; kp_.ld = d_.ld; kp_.lh = d_.lh;
+    kp_.nx2 = d_.nx2; kp_.ny2 = d_.ny2; kp_.ld_big = d_.ld_big; kp_.K = d_.K;
+    kp_.plane = (long long)d_.ld * ny;
+    kp_.plane_big = (long long)d_.ld_big * d_.ny2;
+    kp_.dx = d_.dx; kp_.dy = d_.dy; kp_.dz = d_.dz;
+    kp_.L_x = d_.p.L_x; kp_.L_y = d_.p.L_y; kp_.L_z = d_.p.L_z;
+    kp_.dt = d_.p.dt; kp_.tadv1 = d_.tadv1; kp_.tadv2 = d_.tadv2;
+    kp_.vonk = d_.p.vonk; kp_.zo = d_.p.zo; kp_.nu = d_.nu; kp_.delta = d_.delta;
+    kp_.lagran_dt = d_.lagran_dt; kp_.mpfx = d_.mpfx; kp_.mpfy = d_.mpfy;
+    kp_.nu_nd = d_.p.nu_molec / (d_.p.z_i * d_.p.u_star);
+    kp_.ubot = d_.p.ubot; kp_.utop = d_.p.utop;
+    kp_.lbc = d_.p.lbc_mom; kp_.ubc = d_.p.ubc_mom; kp_.use_mpf = d_.p.use_mean_p_force;
+    kp_.turbines = d_.turbines.empty() ? 0 : 1;
+    nfield_ = (long long)(nz + 1) * kp_.plane;
+    for (int f = 0; f < LESGO_NFIELDS; ++f) F_[f] = alloc<R>(nfield_);
+    for (int f = 0; f < 4; ++f) Ftmp_[f] = alloc<R>(nfield_);
+    for (int f = 0; f < 4; ++f) wall_[f] = alloc<R>(kp_.plane);
+    fza_uv_ = kp_.turbines ? alloc<R>(nfield_) : nullptr;
+    for (int f = 0; f < 6; ++f) big_[f] = alloc<R>((long long)(nz + 1) * kp_.plane_big);
+    vol_s_ = (long long)nz * ny * d_.K;
+    vol_b_ = (long long)nz * d_.ny2 * d_.K;
+    specA_ = alloc<T2>(std::max({21 * vol_s_, 6 * vol_s_, 3 * vol_b_}));
+    specB_ = alloc<T2>(std::max({42 * vol_s_, 6 * vol_b_, 9 * vol_s_}));
+    specC_ = alloc<T2>(4LL * ny * d_.K);
+    const long long pl_s = (long long)ny * d_.K;
+    hspec_ = alloc<double2>(3 * vol_s_);
+    hplane_ = alloc<double2>(2 * pl_s);
+    phat_ = alloc<double2>((nz + 1) * pl_s);
+    gam_ = alloc<double>((nz + 2) * pl_s);
+    err_ = alloc<int>(1);
+    build_tables();
+    if (kp_.turbines) build_turbines();
+    CK(cudaStreamSynchronize(st_));
+  }
+
+  ~Solver() override {
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    for (void* p : allocs_) cudaFree(p);
+    if (st_) cudaStreamDestroy(st_);
+  }
+
+  const Derived& der() const override { return d_; }
+
+  // ---------------- field access -----------------------------------------
+  void check_range(int f, int lbz, int nzhi) const {
+    if (f < 0 || f >= LESGO_NFIELDS) throw Error(LESGO_ERR_ARG, "bad field id");
+    if (lbz < 0 || nzhi > d_.nz || nzhi < lbz) throw Error(LESGO_ERR_ARG, "levels outside 0..nz");
+  }
+  void set_field(int f, const double* h, int lbz, int nzhi) override {
+    check_range(f, lbz, nzhi);
+    const long long n = (long long)(nzhi - lbz + 1) * kp_.plane;
+    R* dst = F_[f] + (long long)lbz * kp_.plane;
+    if (std::is_same<R, double>::value) {
+      CK(cudaMemcpyAsync(dst, h, n * sizeof(double), cudaMemcpyHostToDevice, st_));
+    } else {
+      double* stg = staging(n);
+      CK(cudaMemcpyAsync(stg, h, n * sizeof(double), cudaMemcpyHostToDevice, st_));
+      k_convert<double, R><<<grid1(n), 256, 0, st_>>>(stg, dst, n);
+      post();
+    }
+    CK(cudaStreamSynchronize(st_));
+  }
+  void get_field(int f, double* h, int lbz, int nzhi) override {
+    check_range(f, lbz, nzhi);
+    const long long n = (long long)(nzhi - lbz + 1) * kp_.plane;
+    const R* src = F_[f] + (long long)lbz * kp_.plane;
+    if (std::is_same<R, double>::value) {
+      CK(cudaMemcpyAsync(h, src, n * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    } else {
+      double* stg = staging(n);
+      k_convert<R, double><<<grid1(n), 256, 0, st_>>>(src, stg, n);
+      post();
+      CK(cudaMemcpyAsync(h, stg, n * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    }
+    CK(cudaStreamSynchronize(st_));
+  }
+
+  void init_ic(uint64_t seed) override {
+    const long long n = nfield_;
+    k_ic<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_, seed);
+    post();
+    CK(cudaStreamSynchronize(st_));
+  }
+
+  // ---------------- stage entry points ------------------------------------
+  void filt_da(int f, int fx, int fy) override {
+    const R sc = (R)(1.0 / ((double)d_.nx * d_.ny));
+    SrcFields<R, 1> src{{F_[f]}, sc, 1, 1, d_.ld, kp_.plane};
+    xfwd<1>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+    ypass_lin<1, 3, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+                                        {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}});
+    DstFields<R, 3> dst{{F_[f], F_[fx], F_[fy]}, 1, 1, d_.ld, kp_.plane};
+    xinv<3>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+  }
+  void ddxy(int f, int fx, int fy) override {
+    const R sc = (R)(1.0 / ((double)d_.nx * d_.ny));
+    SrcFields<R, 1> src{{F_[f]}, sc, 1, 1, d_.ld, kp_.plane};
+    xfwd<1>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+    if (fx >= 0 && fy >= 0) {
+      ypass_lin<1, 2, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+                                          {{MUL_IKX}, {MUL_IKY}});
+      DstFields<R, 2> dst{{F_[fx], F_[fy]}, 1, 1, d_.ld, kp_.plane};
+      xinv<2>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    } else {
+      ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+                                          {{fx >= 0 ? MUL_IKX : MUL_IKY}});
+      DstFields<R, 1> dst{{F_[fx >= 0 ? fx : fy]}, 1, 1, d_.ld, kp_.plane};
+      xinv<1>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    }
+  }
+  void ddz(int f, int dfdz, bool uv) override {
+    const long long n = (long long)d_.nx * d_.ny * d_.nz;
+    if (uv) k_ddz<R, true><<<grid1(n), 256, 0, st_>>>(F_[f], F_[dfdz], kp_);
+    else k_ddz<R, false><<<grid1(n), 256, 0, st_>>>(F_[f], F_[dfdz], kp_);
+    post();
+  }
+  void test_filter(int f, int level) override {
+    if (level < 0 || level > d_.nz) throw Error(LESGO_ERR_ARG, "level");
+    filter_planes(F_[f], F_[f], level, F_[f] + (long long)level * kp_.plane, F_[f] + (long long)level * kp_.plane, 1);
+  }
+  void wallstress() override {
+    wall_planes();
+    const int n = d_.nx * d_.ny;
+    k_wall<R><<<(n + 255) / 256, 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], wall_[0], wall_[1], wall_[2], wall_[3],
+                                                F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_DUDZ], F_[LESGO_DVDZ], kp_);
+    post();
+  }
+  void sgs_stag() override {
+    const bool cs_fill = (jt_ == 1 && !d_.p.initu);
+    const bool lag = !cs_fill && (jt_ >= d_.p.dyn_init || d_.p.initu) && (jt_total_ % d_.p.cs_count == 0);
+    if (!lag) {
+      column<COL_STORE_S | COL_TAU>(cs_fill);
+    } else {
+      column<COL_STORE_S>(false);
+      lagrange();
+      column<COL_READ_S | COL_TAU>(false);
+    }
+  }
+  void divstress(int which) override {
+    const R sc = (R)(1.0 / ((double)d_.nx * d_.ny));
+    const R idz = (R)(1.0 / d_.dz);
+    if (which == 3) {
+      SrcFields<R, 5> src{{F_[LESGO_TXX], F_[LESGO_TXY], F_[LESGO_TYY], F_[LESGO_TXZ], F_[LESGO_TYZ]}, sc, 1, 1, d_.ld, kp_.plane};
+      xfwd<5>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+      ypass_lin<5, 3, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+                                          {{MUL_IKX, MUL_IKY, 0, 0, 0}, {0, MUL_IKX, MUL_IKY, 0, 0}, {0, 0, 0, MUL_IKX, MUL_IKY}});
+      DstDiv<R, 3> dst{F_[LESGO_DIVTX], F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_TZZ],
+                       idz, d_.ld, d_.nz, kp_.plane};
+      xinv<3>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    } else if (which == 1) {
+      SrcFields<R, 3> src{{F_[LESGO_TXX], F_[LESGO_TXY], F_[LESGO_TYY]}, sc, 1, 1, d_.ld, kp_.plane};
+      xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+      ypass_lin<3, 2, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+                                          {{MUL_IKX, MUL_IKY, 0}, {0, MUL_IKX, MUL_IKY}});
+      DstDiv<R, 1> dst{F_[LESGO_DIVTX], F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_TZZ],
+                       idz, d_.ld, d_.nz, kp_.plane};
+      xinv<2>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    } else {
+      SrcFields<R, 2> src{{F_[LESGO_TXZ], F_[LESGO_TYZ]}, sc, 1, 1, d_.ld, kp_.plane};
+      xfwd<2>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+      ypass_lin<2, 1, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+                                          {{MUL_IKX, MUL_IKY}});
+      DstDiv<R, 2> dst{F_[LESGO_DIVTX], F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_TZZ],
+                       idz, d_.ld, d_.nz, kp_.plane};
+      xinv<1>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    }
+  }
+  void convec() override { convec_impl(false, false); }
+  void turbines_forcing() override {
+    if (!kp_.turbines) return;
+    turb_impl();
+  }
+  void begin_step() override {
+    ++jt_; ++jt_total_;
+    for (int c = 0; c < 3; ++c)
+      CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c], F_[LESGO_RHSX + c], nfield_ * sizeof(R), cudaMemcpyDeviceToDevice, st_));
+  }
+  void rhs_assemble() override {
+    const long long n = kp_.plane * d_.nz;
+    k_rhs_assemble<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_RHSZ], F_[LESGO_DIVTX],
+                                                 F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_FXA], F_[LESGO_FYA], F_[LESGO_FZA], kp_);
+    post();
+  }
+  void ab2() override {
+    if (jt_total_ == 1 && !d_.p.initu)
+      for (int c = 0; c < 3; ++c)
+        CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c], F_[LESGO_RHSX + c], nfield_ * sizeof(R), cudaMemcpyDeviceToDevice, st_));
+    const long long n = kp_.plane * d_.nz;
+    k_ab2<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_RHSZ],
+                                        F_[LESGO_RHSX_F], F_[LESGO_RHSY_F], F_[LESGO_RHSZ_F], kp_);
+    post();
+  }
+  void press_stag_array() override { pressure_impl(false); }
+  void rhs_sub_dp() override {
+    const long long n = kp_.plane * d_.nz;
+    k_rhs_sub_dp<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_RHSZ], F_[LESGO_DPDX],
+                                               F_[LESGO_DPDY], F_[LESGO_DPDZ], kp_);
+    post();
+  }
+  void project() override {
+    const long long n = (long long)d_.nx * d_.ny * d_.nz;
+    k_project<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_DPDZ], F_[LESGO_U], F_[LESGO_V],
+                                            F_[LESGO_W], kp_);
+    post();
+    k_project_bc<R><<<grid1(kp_.plane), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_);
+    post();
+  }
+
+  // ---------------- fused time loop ------------------------------------------
+  void step(int nsteps) override {
+    for (int s = 0; s < nsteps; ++s) {
+      ++jt_; ++jt_total_;
+      const bool inilag = !d_.p.initu;
+      StepKey key;
+      key.euler = (jt_total_ == 1 && !d_.p.initu);
+      key.cs_fill = (jt_ == 1 && inilag);
+      key.lag = !key.cs_fill && (jt_ >= d_.p.dyn_init || d_.p.initu) && (jt_total_ % d_.p.cs_count == 0);
+      key.init_lm = key.lag && inilag && !F_LM_MM_init_ && (jt_ == d_.p.cs_count || jt_ == d_.p.dyn_init);
+      key.init_qn = key.lag && inilag && !F_QN_NN_init_ && (jt_ == d_.p.cs_count || jt_ == d_.p.dyn_init);
+      const bool steady = !key.euler && !key.cs_fill && !key.init_lm && !key.init_qn;
+      const int code = key.code();
+      if (steady && use_graphs_) {
+        auto it = graphs_.find(code);
+        if (it == graphs_.end()) {
+          cudaGraph_t g;
+          launches_ = 0;
+          CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+          try {
+            step_body(key);
+          } catch (...) {
+            cudaStreamEndCapture(st_, &g);
+            throw;
+          }
+          CK(cudaStreamEndCapture(st_, &g));
+          cudaGraphExec_t ge;
+          CK(cudaGraphInstantiate(&ge, g, 0));
+          cudaGraphDestroy(g);
+          graphs_[code] = ge;
+          launch_count_[code] = launches_;
+          it = graphs_.find(code);
+        }
+        CK(cudaGraphLaunch(it->second, st_));
+      } else {
+        launches_ = 0;
+        step_body(key);
+        launch_count_[code] = launches_;
+      }
+      if (key.init_lm) F_LM_MM_init_ = true;
+      if (key.init_qn) F_QN_NN_init_ = true;
+    }
+  }
+
+  int sync() override {
+    CK(cudaStreamSynchronize(st_));
+    int e = 0;
+    CK(cudaMemcpy(&e, err_, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+      CK(cudaMemset(err_, 0, sizeof(int)));
+      return LESGO_ERR_NUMERIC;
+    }
+    return LESGO_OK;
+  }
+
+  void diag(double* out) override {
+    const int nb = 4 * 152;
+    if (!diag_part_) { diag_part_ = alloc<double>(nb * 7); diag_out_ = alloc<double>(8); }
+    k_diag<R><<<nb, 256, 0, st_>>>(F_[LESGO_DUDX], F_[LESGO_DVDY], F_[LESGO_DWDZ], F_[LESGO_U], F_[LESGO_V], F_[LESGO_W],
+                                   F_[LESGO_TXZ], F_[LESGO_TYZ], kp_, diag_part_);
+    post();
+    k_diag_final<<<1, 32, 0, st_>>>(diag_part_, nb, diag_out_);
+    post();
+    double h[7];
+    CK(cudaMemcpyAsync(h, diag_out_, 7 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    const double npts = (double)d_.nx * d_.ny * (d_.nz - 1);
+    out[0] = h[0] / npts;
+    out[1] = h[1] * 0.5 / npts;
+    out[2] = d_.p.dt * std::max({h[2] / d_.dx, h[3] / d_.dy, h[4] / d_.dz});
+    const double nxy = (double)d_.nx * d_.ny;
+    out[3] = std::sqrt((h[5] / nxy) * (h[5] / nxy) + (h[6] / nxy) * (h[6] / nxy));
+  }
+
+  void counters(int* jt, int* jt_total) const override {
+    if (jt) *jt = jt_;
+    if (jt_total) *jt_total = jt_total_;
+  }
+
+  void turbine_state(double* udT, double* fn, double* pw, int n) override {
+    const int m = std::min(n, th_.n);
+    std::vector<double> a(th_.n), b(th_.n);
+    if (th_.n) {
+      CK(cudaStreamSynchronize(st_));
+      CK(cudaMemcpy(a.data(), td_.u_d_T, th_.n * sizeof(double), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(b.data(), td_.f_n, th_.n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    for (int s = 0; s < m; ++s) {
+      if (udT) udT[s] = a[s];
+      if (fn) fn[s] = b[s];
+      if (pw) pw[s] = -b[s] * a[s];
+    }
+  }
+
+  int launches_per_step(int with_sgs) const override {
+    for (auto& kv : launch_count_) {
+      StepKey k = StepKey::from(kv.first);
+      if (k.lag == (with_sgs != 0) && !k.euler && !k.cs_fill && !k.init_lm && !k.init_qn) return kv.second;
+    }
+    return -1;
+  }
+
+ private:
+  struct StepKey {
+    bool euler = false, cs_fill = false, lag = false, init_lm = false, init_qn = false;
+    int code() const { return euler | (cs_fill << 1) | (lag << 2) | (init_lm << 3) | (init_qn << 4); }
+    static StepKey from(int c) {
+      StepKey k;
+      k.euler = c & 1; k.cs_fill = c & 2; k.lag = c & 4; k.init_lm = c & 8; k.init_qn = c & 16;
+      return k;
+    }
+  };
+
+  void step_body(const StepKey& key) {
+    // main.f90:155-172: derivatives (RHS_f is saved inside the fused convec epilogue)
+    SrcFields<R, 3> src{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, (R)(1.0 / ((double)d_.nx * d_.ny)), 1, 1, d_.ld, kp_.plane};
+    xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+    ypass_lin<1, 3, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 3, ROW_SAME,
+                                        {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}});
+    DstFields<R, 9> dst{{F_[LESGO_U], F_[LESGO_DUDX], F_[LESGO_DUDY], F_[LESGO_V], F_[LESGO_DVDX], F_[LESGO_DVDY],
+                         F_[LESGO_W], F_[LESGO_DWDX], F_[LESGO_DWDY]}, 1, 1, d_.ld, kp_.plane};
+    xinv<9>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    // wall model inputs (test-filtered first level), main.f90:180-189
+    wall_planes();
+    // applied forcing uses the filtered velocity of this step (main.f90:248-257)
+    if (kp_.turbines) turb_impl();
+    // sgs_stag with ddz_uv/ddz_w and the wall values fused (main.f90:164-189)
+    if (!key.lag) {
+      column<COL_DDZ | COL_TAU>(key.cs_fill);
+    } else {
+      column<COL_DDZ | COL_STORE_S>(false);
+      lagrange(key.init_lm, key.init_qn);
+      column<COL_READ_S | COL_TAU>(false);
+    }
+    divstress(3);
+    convec_impl(true, key.euler);
+    pressure_impl(true);
+  }
+
+  // ---------------- building blocks ----------------------------------------
+  template <typename T>
+  T* alloc(long long n) {
+    void* p = nullptr;
+    CK(cudaMalloc(&p, std::max<long long>(n, 1) * sizeof(T)));
+    CK(cudaMemsetAsync(p, 0, std::max<long long>(n, 1) * sizeof(T), st_));
+    allocs_.push_back(p);
+    return (T*)p;
+  }
+  double* staging(long long n) {
+    if (n > staging_n_) {
+      staging_ = alloc<double>(nfield_);
+      staging_n_ = nfield_;
+    }
+    return staging_;
+  }
+  static dim3 grid1(long long n) { return dim3((unsigned)((n + 255) / 256)); }
+  void post() {
+    ++launches_;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error(LESGO_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  }
+  template <typename KF>
+  static void set_smem(KF kern, size_t bytes) {
+    if (bytes > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      if (e != cudaSuccess) throw Error(LESGO_ERR_CUDA, std::string("smem attribute: ") + cudaGetErrorString(e));
+    }
+  }
+
+  FftPlan<R> make_plan(int n) {
+    FftPlan<R> p{};
+    p.n = n;
+    auto r = factorize(n);
+    p.nf = (int)r.size();
+    for (int i = 0; i < p.nf; ++i) p.radix[i] = r[i];
+    std::vector<T2> tw(n), rtw(n + 1);
+    for (int t = 0; t < n; ++t) {
+      const long double a = -2.0L * kPiL * (long double)t / (long double)n;
+      tw[t] = mkc((R)cosl(a), (R)sinl(a));
+    }
+    for (int k = 0; k <= n; ++k) {
+      const long double a = -2.0L * kPiL * (long double)k / (long double)(2 * n);
+      rtw[k] = mkc((R)cosl(a), (R)sinl(a));
+    }
+    T2* dtw = alloc<T2>(n);
+    T2* drtw = alloc<T2>(n + 1);
+    CK(cudaMemcpyAsync(dtw, tw.data(), n * sizeof(T2), cudaMemcpyHostToDevice, st_));
+    CK(cudaMemcpyAsync(drtw, rtw.data(), (n + 1) * sizeof(T2), cudaMemcpyHostToDevice, st_));
+    CK(cudaStreamSynchronize(st_));
+    p.tw = dtw;
+    p.rtw = drtw;
+    return p;
+  }
+
+  void build_tables() {
+    px_ = make_plan(d_.nx / 2);
+    py_ = make_plan(d_.ny);
+    pxb_ = make_plan(d_.nx2 / 2);
+    pyb_ = make_plan(d_.ny2);
+    // wavenumbers (fft.f90:130-160) for kx < nx/2 and every ky row
+    const int ny = d_.ny, lh = d_.lh;
+    std::vector<double> kx(d_.K), ky(ny);
+    for (int jx = 0; jx < d_.K; ++jx) kx[jx] = 2.0 * kPi / d_.p.L_x * (double)jx;
+    for (int jy = 0; jy < ny; ++jy) {
+      const int m = ((jy + ny / 2) % ny) - ny / 2;
+      ky[jy] = (jy == ny / 2) ? 0.0 : 2.0 * kPi / d_.p.L_y * (double)m;
+    }
+    // test-filter kernels (test_filtermodule.f90:38-123), (ny, lh)
+    std::vector<double> G1((size_t)ny * lh), G2((size_t)ny * lh);
+    for (int jy = 0; jy < ny; ++jy)
+      for (int jx = 0; jx < lh; ++jx) {
+        double kxv = (jx < lh - 1 && jy != ny / 2) ? 2.0 * kPi / d_.p.L_x * (double)jx : 0.0;
+        const int m = ((jy + ny / 2) % ny) - ny / 2;
+        double kyv = (jx < lh - 1 && jy != ny / 2) ? 2.0 * kPi / d_.p.L_y * (double)m : 0.0;
+        volatile double k2 = kxv * kxv;
+        k2 = k2 + kyv * kyv;
+        for (int f = 0; f < 2; ++f) {
+          const double alpha = f == 0 ? 2.0 : 4.0;
+          const double dtest = alpha * std::sqrt(d_.dx * d_.dy);
+          const double kc2 = (kPi / dtest) * (kPi / dtest);
+          double g = 1.0 / ((double)d_.nx * d_.ny);
+          if (k2 >= kc2) g = 0.0;
+          if (jx == lh - 1 || jy == ny / 2) g = 0.0;
+          (f == 0 ? G1 : G2)[(size_t)jy * lh + jx] = g;
+        }
+      }
+    kxw_ = upload_as<R>(kx);
+    kyw_ = upload_as<R>(ky);
+    kxw64_ = upload_as<double>(kx);
+    kyw64_ = upload_as<double>(ky);
+    G1_ = upload_as<R>(G1);
+    G2_ = upload_as<R>(G2);
+  }
+  template <typename T>
+  T* upload_as(const std::vector<double>& v) {
+    std::vector<T> t(v.begin(), v.end());
+    T* p = alloc<T>((long long)t.size());
+    CK(cudaMemcpyAsync(p, t.data(), t.size() * sizeof(T), cudaMemcpyHostToDevice, st_));
+    CK(cudaStreamSynchronize(st_));
+    return p;
+  }
+  template <typename T>
+  T* upload_vec(const std::vector<T>& v) {
+    T* p = alloc<T>((long long)v.size());
+    if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st_));
+    CK(cudaStreamSynchronize(st_));
+    return p;
+  }
+
+  void build_turbines() {
+    th_ = turbines_init_host(d_);
+    td_.nturb = th_.n;
+    td_.node_off = upload_vec(th_.node_off);
+    td_.node_q = upload_vec(th_.node_q);
+    td_.node_ind = upload_vec(th_.node_ind);
+    td_.win_turb = upload_vec(th_.win_turb);
+    td_.win_q = upload_vec(th_.win_q);
+    td_.win_ind = upload_vec(th_.win_ind);
+    td_.nwin = (int)th_.win_q.size();
+    td_.nhat = upload_vec(th_.nhat);
+    td_.ctp = upload_vec(th_.ctp);
+    td_.corr = upload_vec(th_.corr);
+    td_.dia = upload_vec(th_.dia);
+    td_.u_d = alloc<double>(th_.n);
+    td_.u_d_T = upload_vec(std::vector<double>(th_.n, d_.p.n_turbines ? -1.0 : 0.0));
+    td_.f_n = alloc<double>(th_.n);
+    td_.disk = alloc<double>(th_.n);
+    const double dt_dim = d_.p.dt * d_.p.z_i / d_.p.u_star;
+    td_.eps = d_.p.T_avg_dim > 0 ? (dt_dim / d_.p.T_avg_dim) / (1. + dt_dim / d_.p.T_avg_dim) : 1.0;
+    td_.dvol = d_.dx * d_.dy * d_.dz;
+    cols_ = upload_vec(th_.cols);
+  }
+
+  template <int NF, class Src>
+  void xfwd(const Src& src, int M, int nyrows, int nlev, T2* out, long long out_fs, const FftPlan<R>& plan) {
+    XfGeom g;
+    g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nlev; g.ls = M / 2 + 1;
+    const int target = sizeof(R) == 8 ? 2048 : 4096;
+    g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
+    g.out_field_stride = out_fs;
+    const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
+    auto kern = k_xfwd<R, NF, Src>;
+    set_smem(kern, smem);
+    kern<<<(g.nrows + g.rpc - 1) / g.rpc, 256, smem, st_>>>(g, plan, src, out);
+    post();
+  }
+
+  template <int NF, class Dst>
+  void xinv(const Dst& dst, const T2* in, long long in_fs, int M, int nyrows, int nlev, const FftPlan<R>& plan) {
+    XiGeom g;
+    g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nlev; g.ls = M / 2 + 1;
+    const int target = sizeof(R) == 8 ? 2048 : 4096;
+    g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
+    g.in_field_stride = in_fs;
+    const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
+    auto kern = k_xinv<R, NF, Dst>;
+    set_smem(kern, smem);
+    kern<<<(g.nrows + g.rpc - 1) / g.rpc, 256, smem, st_>>>(g, plan, in, dst);
+    post();
+  }
+
+  // Y pass over groups of NIN inputs -> NOUT outputs.
+  template <int NIN, int NOUT, bool FWD, bool INV, typename InT, typename OutT>
+  void ypass_lin(const InT* in, long long in_fs, int in_lev0, int in_levstride, int in_rows, OutT* out, long long out_fs,
+                 int out_rows, int nlev, int ngroups, int rowmode, std::initializer_list<std::initializer_list<int>> mul) {
+    YOpLin<R, NIN, NOUT, InT, OutT> op;
+    op.in = in; op.in_fs = in_fs; op.in_lev0 = in_lev0; op.in_levstride = in_levstride; op.in_rows = in_rows;
+    op.out = out; op.out_fs = out_fs; op.out_rows = out_rows;
+    op.K = d_.K; op.lh = d_.lh; op.ny_small = d_.ny; op.ny_big = d_.ny2; op.rowmode = rowmode;
+    int o = 0;
+    for (auto& row : mul) {
+      int i = 0;
+      for (int m : row) { if (o < NOUT && i < NIN) op.mul[o][i] = m; ++i; }
+      for (; i < NIN; ++i) op.mul[o][i] = MUL_ZERO;
+      ++o;
+    }
+    op.kxw = kxw_; op.kyw = kyw_; op.G1 = G1_; op.G2 = G2_;
+    YGeom g;
+    g.ny_in = in_rows; g.ny_out = out_rows; g.K = d_.K; g.nlev = nlev;
+    g.ls_in = in_rows + 1; g.ls_out = out_rows + 1;
+    const FftPlan<R>& pin = (in_rows == d_.ny) ? py_ : pyb_;
+    const FftPlan<R>& pout = (out_rows == d_.ny) ? py_ : pyb_;
+    const size_t budget = 110 * 1024;
+    int tk = sizeof(R) == 8 ? 8 : 16;
+    auto smem_of = [&](int t) {
+      const size_t s = (size_t)NIN * t * g.ls_in;
+      return (s + std::max(s, (size_t)2 * t * g.ls_out)) * sizeof(T2);
+    };
+    while (tk > 1 && smem_of(tk) > budget) tk /= 2;
+    tk = std::min(tk, d_.K);
+    g.tk = tk;
+    g.in_lev_stride = 0; g.out_lev_stride = 0;
+    const size_t smem = smem_of(tk);
+    auto kern = k_ypass<R, NIN, NOUT, FWD, INV, YOpLin<R, NIN, NOUT, InT, OutT>>;
+    set_smem(kern, smem);
+    dim3 grid((d_.K + tk - 1) / tk, nlev, ngroups);
+    kern<<<grid, 256, smem, st_>>>(g, pin, pout, op);
+    post();
+  }
+
+  // test-filter (G_test) of one plane of two fields into two (ld, ny) planes
+  void filter_planes(const R* a, const R* b, int level, R* oa, R* ob, int nf) {
+    SrcFields<R, 2> src{{a, b}, (R)1, level, 1, d_.ld, kp_.plane};
+    xfwd<2>(src, d_.nx, d_.ny, 1, specC_, (long long)d_.ny * d_.K, px_);
+    ypass_lin<1, 1, true, true, T2, T2>(specC_, (long long)d_.ny * d_.K, 0, 1, d_.ny, specC_ + 2LL * d_.ny * d_.K,
+                                        (long long)d_.ny * d_.K, d_.ny, 1, 2, ROW_SAME, {{MUL_G1}});
+    if (nf == 1) {
+      DstFields<R, 1> dst{{oa}, 0, 1, d_.ld, 0};
+      xinv<1>(dst, specC_ + 2LL * d_.ny * d_.K, (long long)d_.ny * d_.K, d_.nx, d_.ny, 1, px_);
+    } else {
+      DstFields<R, 2> dst{{oa, ob}, 0, 1, d_.ld, 0};
+      xinv<2>(dst, specC_ + 2LL * d_.ny * d_.K, (long long)d_.ny * d_.K, d_.nx, d_.ny, 1, px_);
+    }
+  }
+  void wall_planes() {
+    if (d_.p.lbc_mom == 2) filter_planes(F_[LESGO_U], F_[LESGO_V], 1, wall_[0], wall_[1], 2);
+    if (d_.p.ubc_mom == 2) filter_planes(F_[LESGO_U], F_[LESGO_V], d_.nz - 1, wall_[2], wall_[3], 2);
+  }
+
+  template <int FLAGS>
+  void column(bool cs_fill) {
+    ColArgs<R> a;
+    a.u = F_[LESGO_U]; a.v = F_[LESGO_V]; a.w = F_[LESGO_W];
+    a.dudx = F_[LESGO_DUDX]; a.dudy = F_[LESGO_DUDY]; a.dvdx = F_[LESGO_DVDX]; a.dvdy = F_[LESGO_DVDY];
+    a.dwdx = F_[LESGO_DWDX]; a.dwdy = F_[LESGO_DWDY];
+    a.dudz = F_[LESGO_DUDZ]; a.dvdz = F_[LESGO_DVDZ]; a.dwdz = F_[LESGO_DWDZ];
+    a.S11 = F_[LESGO_S11]; a.S12 = F_[LESGO_S12]; a.S13 = F_[LESGO_S13];
+    a.S22 = F_[LESGO_S22]; a.S23 = F_[LESGO_S23]; a.S33 = F_[LESGO_S33];
+    a.Cs = F_[LESGO_CS_OPT2];
+    a.txx = F_[LESGO_TXX]; a.txy = F_[LESGO_TXY]; a.txz = F_[LESGO_TXZ];
+    a.tyy = F_[LESGO_TYY]; a.tyz = F_[LESGO_TYZ]; a.tzz = F_[LESGO_TZZ];
+    a.wb_u = wall_[0]; a.wb_v = wall_[1]; a.wt_u = wall_[2]; a.wt_v = wall_[3];
+    a.kp = kp_;
+    a.delta2 = d_.delta * d_.delta;
+    a.chunk = 16;
+    a.cs_fill = cs_fill ? 1 : 0;
+    const int ncol = d_.nx * d_.ny;
+    dim3 grid((ncol + 255) / 256, (d_.nz + a.chunk - 1) / a.chunk);
+    k_column<R, FLAGS><<<grid, 256, 0, st_>>>(a);
+    post();
+    if (cs_fill && !(FLAGS & COL_TAU)) {
+      k_fill<R><<<grid1(nfield_), 256, 0, st_>>>(F_[LESGO_CS_OPT2], nfield_, (R)0.03);
+      post();
+    }
+  }
+
+  void lagrange(bool init_lm, bool init_qn) {
+    InterpArgs<R> ia;
+    ia.u = F_[LESGO_U]; ia.v = F_[LESGO_V]; ia.w = F_[LESGO_W];
+    const int Fi[4] = {LESGO_F_LM, LESGO_F_MM, LESGO_F_QN, LESGO_F_NN};
+    for (int f = 0; f < 4; ++f) { ia.Fin[f] = F_[Fi[f]]; ia.Fout[f] = Ftmp_[f]; }
+    ia.kp = kp_;
+    const long long n = (long long)d_.nx * d_.ny * d_.nz;
+    k_interp<R><<<grid1(n), 256, 0, st_>>>(ia);
+    post();
+    SrcLagrange<R> src{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_S11], F_[LESGO_S12], F_[LESGO_S13],
+                       F_[LESGO_S22], F_[LESGO_S23], F_[LESGO_S33], d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane};
+    xfwd<21>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+    ypass_lin<1, 2, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 21, ROW_SAME,
+                                        {{MUL_G1}, {MUL_G2}});
+    DstLagrange<R> dst;
+    dst.FLMi = Ftmp_[0]; dst.FMMi = Ftmp_[1]; dst.FQNi = Ftmp_[2]; dst.FNNi = Ftmp_[3];
+    dst.FLM = F_[LESGO_F_LM]; dst.FMM = F_[LESGO_F_MM]; dst.FQN = F_[LESGO_F_QN]; dst.FNN = F_[LESGO_F_NN];
+    dst.Cs = F_[LESGO_CS_OPT2]; dst.Beta = F_[LESGO_BETA]; dst.Tn_all = F_[LESGO_TN_ALL]; dst.ee_now = F_[LESGO_EE_NOW];
+    dst.cst = 2.0 * (d_.delta * d_.delta);
+    dst.opftdelta = 1.5 * d_.delta;
+    dst.lagran_dt = d_.lagran_dt;
+    dst.beta_exp = std::log(2.0) / (std::log(4.0) - std::log(2.0));
+    dst.ld = d_.ld; dst.nz = d_.nz; dst.lbc = kp_.lbc; dst.ubc = kp_.ubc;
+    dst.init_lm = init_lm; dst.init_qn = init_qn;
+    dst.plane = kp_.plane;
+    xinv<42>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+  }
+  void lagrange() {
+    const bool inilag = !d_.p.initu;
+    const bool init_lm = inilag && !F_LM_MM_init_ && (jt_ == d_.p.cs_count || jt_ == d_.p.dyn_init);
+    const bool init_qn = inilag && !F_QN_NN_init_ && (jt_ == d_.p.cs_count || jt_ == d_.p.dyn_init);
+    lagrange(init_lm, init_qn);
+    if (init_lm) F_LM_MM_init_ = true;
+    if (init_qn) F_QN_NN_init_ = true;
+  }
+
+  void convec_impl(bool fused, bool euler) {
+    const R c = (R)(1.0 / ((double)d_.nx * d_.ny));
+    SrcVort<R> sv{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDY], F_[LESGO_DUDZ], F_[LESGO_DVDX],
+                  F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane};
+    xfwd<6>(sv, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+    ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_b_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}});
+    DstFields<R, 6> db{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld_big, kp_.plane_big};
+    xinv<6>(db, specB_, vol_b_, d_.nx2, d_.ny2, d_.nz, pxb_);
+    const R cb = (R)(1.0 / ((double)d_.nx2 * d_.ny2));
+    SrcConvProd<R> sp{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5], cb, d_.ld_big, d_.nz, kp_.plane_big};
+    xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, specA_, vol_b_, pxb_);
+    ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_b_, 0, 1, d_.ny2, specB_, vol_s_, d_.ny, d_.nz, 3, ROW_UNPAD, {{MUL_ONE}});
+    if (!fused) {
+      DstConvec<R, false> dc{};
+      dc.RHSx = F_[LESGO_RHSX]; dc.RHSy = F_[LESGO_RHSY]; dc.RHSz = F_[LESGO_RHSZ];
+      dc.ld = d_.ld; dc.nz = d_.nz; dc.plane = kp_.plane;
+      xinv<3>(dc, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    } else {
+      DstConvec<R, true> dc{};
+      dc.RHSx = F_[LESGO_RHSX]; dc.RHSy = F_[LESGO_RHSY]; dc.RHSz = F_[LESGO_RHSZ];
+      dc.RHSxf = F_[LESGO_RHSX_F]; dc.RHSyf = F_[LESGO_RHSY_F]; dc.RHSzf = F_[LESGO_RHSZ_F];
+      dc.u = F_[LESGO_U]; dc.v = F_[LESGO_V]; dc.w = F_[LESGO_W];
+      dc.divtx = F_[LESGO_DIVTX]; dc.divty = F_[LESGO_DIVTY]; dc.divtz = F_[LESGO_DIVTZ];
+      dc.fxa = F_[LESGO_FXA]; dc.fya = F_[LESGO_FYA]; dc.fza = F_[LESGO_FZA];
+      dc.dt = d_.p.dt; dc.t1 = d_.tadv1; dc.t2 = d_.tadv2; dc.mpfx = d_.mpfx; dc.mpfy = d_.mpfy;
+      dc.ld = d_.ld; dc.nz = d_.nz; dc.euler = euler ? 1 : 0; dc.use_mpf = d_.p.use_mean_p_force; dc.turbines = kp_.turbines;
+      dc.plane = kp_.plane;
+      xinv<3>(dc, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    }
+  }
+
+  void pressure_impl(bool fused) {
+    const int nz = d_.nz, ny = d_.ny;
+    const long long pl_s = (long long)ny * d_.K;
+    const double c1 = 1.0 / ((double)d_.nx * d_.ny);
+    const R c2 = (R)(c1 / d_.tadv1 / d_.p.dt);
+    SrcFields<R, 3> su{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, c2, 1, 1, d_.ld, kp_.plane};
+    xfwd<3>(su, d_.nx, ny, nz, specA_, vol_s_, px_);
+    SrcFields<R, 1> sd{{F_[LESGO_DIVTZ]}, (R)c1, 1, nz - 1, d_.ld, kp_.plane};
+    xfwd<1>(sd, d_.nx, ny, 2, specC_, 2 * pl_s, px_);
+    ypass_lin<1, 1, true, false, T2, double2>(specA_, vol_s_, 0, 1, ny, hspec_, vol_s_, ny, nz, 3, ROW_SAME, {{MUL_ONE}});
+    ypass_lin<1, 1, true, false, T2, double2>(specC_, 2 * pl_s, 0, 1, ny, hplane_, 2 * pl_s, ny, 2, 1, ROW_SAME, {{MUL_ONE}});
+    ThomasArgs ta;
+    ta.Hx = hspec_; ta.Hy = hspec_ + vol_s_; ta.Hz = hspec_ + 2 * vol_s_;
+    ta.Hb = hplane_; ta.Ht = hplane_ + pl_s;
+    ta.phat = phat_; ta.gam = gam_;
+    ta.kxw = kxw64_; ta.kyw = kyw64_;
+    ta.dz = d_.dz; ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.err = err_;
+    k_thomas<<<(unsigned)((pl_s + 127) / 128), 128, 0, st_>>>(ta);
+    post();
+    // p, i kx p, i ky p at levels 1..nz-1; p at levels 0 and nz
+    ypass_lin<1, 3, false, true, double2, T2>(phat_, 0, 1, 1, ny, specB_, vol_s_, ny, nz - 1, 1, ROW_SAME,
+                                              {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}});
+    ypass_lin<1, 1, false, true, double2, T2>(phat_, 0, 0, nz, ny, specC_, 2 * pl_s, ny, 2, 1, ROW_SAME, {{MUL_ONE}});
+    if (fused) {
+      DstPress<R, true> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U], F_[LESGO_V],
+                           d_.p.dt, d_.tadv1, d_.ld, kp_.plane};
+      xinv<3>(dp, specB_, vol_s_, d_.nx, ny, nz - 1, px_);
+    } else {
+      DstPress<R, false> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U], F_[LESGO_V],
+                            d_.p.dt, d_.tadv1, d_.ld, kp_.plane};
+      xinv<3>(dp, specB_, vol_s_, d_.nx, ny, nz - 1, px_);
+    }
+    DstFields<R, 1> d0{{F_[LESGO_P]}, 0, nz, d_.ld, kp_.plane};
+    xinv<1>(d0, specC_, 2 * pl_s, d_.nx, ny, 2, px_);
+    const long long n = (long long)d_.nx * ny * nz;
+    if (fused)
+      k_wproj<R, true><<<grid1(n), 256, 0, st_>>>(F_[LESGO_P], F_[LESGO_DPDZ], F_[LESGO_RHSZ], F_[LESGO_U], F_[LESGO_V],
+                                                  F_[LESGO_W], kp_);
+    else
+      k_wproj<R, false><<<grid1(n), 256, 0, st_>>>(F_[LESGO_P], F_[LESGO_DPDZ], F_[LESGO_RHSZ], F_[LESGO_U], F_[LESGO_V],
+                                                   F_[LESGO_W], kp_);
+    post();
+  }
+
+  void turb_impl() {
+    k_turb_disk<R><<<th_.n, 256, 0, st_>>>(td_, F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_.plane, d_.nz);
+    post();
+    if (td_.nwin > 0) {
+      k_turb_scatter<R><<<(td_.nwin + 255) / 256, 256, 0, st_>>>(td_, F_[LESGO_FXA], F_[LESGO_FYA], fza_uv_);
+      post();
+      const long long n = (long long)th_.cols.size() * d_.nz;
+      k_turb_fzw<R><<<grid1(n), 256, 0, st_>>>(fza_uv_, F_[LESGO_FZA], cols_, (int)th_.cols.size(), kp_);
+      post();
+    }
+  }
+
+  Derived d_;
+  KP kp_{};
+  cudaStream_t st_ = nullptr;
+  std::vector<void*> allocs_;
+  long long nfield_ = 0, vol_s_ = 0, vol_b_ = 0;
+  R* F_[LESGO_NFIELDS] = {};
+  R* Ftmp_[4] = {};
+  R* wall_[4] = {};
+  R* big_[6] = {};
+  R* fza_uv_ = nullptr;
+  T2 *specA_ = nullptr, *specB_ = nullptr, *specC_ = nullptr;
+  double2 *hspec_ = nullptr, *hplane_ = nullptr, *phat_ = nullptr;
+  double* gam_ = nullptr;
+  int* err_ = nullptr;
+  double *diag_part_ = nullptr, *diag_out_ = nullptr;
+  double* staging_ = nullptr;
+  long long staging_n_ = 0;
+  FftPlan<R> px_{}, py_{}, pxb_{}, pyb_{};
+  R *kxw_ = nullptr, *kyw_ = nullptr, *G1_ = nullptr, *G2_ = nullptr;
+  double *kxw64_ = nullptr, *kyw64_ = nullptr;
+  TurbineHost th_;
+  TurbDev td_{};
+  long long* cols_ = nullptr;
+  int jt_ = 0, jt_total_ = 0;
+  bool F_LM_MM_init_ = false, F_QN_NN_init_ = false;
+  bool use_graphs_ = true;
+  int launches_ = 0;
+  std::map<int, cudaGraphExec_t> graphs_;
+  std::map<int, int> launch_count_;
+};
+
+}  // namespace lesgo
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct lesgo_handle {
+  std::unique_ptr<lesgo::SolverBase> s;
+  std::string err;
+  struct Bind { double* ptr = nullptr; int lbz = 0, nzhi = -1; };
+  Bind bind[LESGO_NFIELDS];
+};
+
+static thread_local std::string g_create_err;
+
+template <typename F>
+static int guarded(lesgo_handle_t* h, F&& fn) {
+  if (!h || !h->s) return LESGO_ERR_ARG;
+  try {
+    fn();
+    return LESGO_OK;
+  } catch (const lesgo::Error& e) {
+    h->err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    h->err = e.what();
+    return LESGO_ERR_CUDA;
+  }
+}
+
+extern "C" {
+
+int lesgo_gpu_params_default(lesgo_params_t* p) {
+  if (!p) return LESGO_ERR_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->nx = 64; p->ny = 64; p->nz_tot = 64;
+  p->L_x = 2.0 * 3.1415926535897932384626433; p->L_y = 3.1415926535897932384626433; p->L_z = 1.0; p->z_i = 1000.0;
+  p->u_star = 0.45; p->vonk = 0.4; p->zo = 1.0e-4; p->dt = 2.0e-4;
+  p->sgs_model = 5; p->cs_count = 5; p->dyn_init = 100; p->ifilter = 1;
+  p->lbc_mom = 2; p->ubc_mom = 0;
+  p->molec = 0; p->nu_molec = 1.14e-5;
+  p->use_mean_p_force = 1; p->eval_mean_p_force = 1;
+  p->mean_p_force_x = 1.0; p->mean_p_force_y = 0.0;
+  p->precision = LESGO_FP64;
+  p->alpha1 = 1.5; p->alpha2 = 1.5; p->filter_cutoff = 1e-2; p->T_avg_dim = -1.0; p->adm_correction = 1;
+  return LESGO_OK;
+}
+
+int lesgo_gpu_create(const lesgo_params_t* p, lesgo_handle_t** h) {
+  if (!p || !h) return LESGO_ERR_ARG;
+  *h = nullptr;
+  try {
+    lesgo::Derived d(*p);
+    auto* hh = new lesgo_handle;
+    try {
+      if (p->precision == LESGO_FP64) hh->s.reset(new lesgo::Solver<double>(d));
+      else hh->s.reset(new lesgo::Solver<float>(d));
+    } catch (...) {
+      delete hh;
+      throw;
+    }
+    *h = hh;
+    return LESGO_OK;
+  } catch (const lesgo::Error& e) {
+    g_create_err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_create_err = e.what();
+    return LESGO_ERR_CUDA;
+  }
+}
+
+int lesgo_gpu_destroy(lesgo_handle_t* h) {
+  if (!h) return LESGO_ERR_ARG;
+  delete h;
+  return LESGO_OK;
+}
+
+const char* lesgo_gpu_last_error(const lesgo_handle_t* h) {
+  if (!h) return g_create_err.c_str();
+  return h->err.c_str();
+}
+
+int lesgo_gpu_dims(const lesgo_handle_t* h, int* nz, int* ld, int* lh, int* nx2, int* ny2) {
+  if (!h || !h->s) return LESGO_ERR_ARG;
+  const auto& d = h->s->der();
+  if (nz) *nz = d.nz;
+  if (ld) *ld = d.ld;
+  if (lh) *lh = d.lh;
+  if (nx2) *nx2 = d.nx2;
+  if (ny2) *ny2 = d.ny2;
+  return LESGO_OK;
+}
+
+int lesgo_gpu_set_field(lesgo_handle_t* h, int f, const double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->set_field(f, host, lbz, nzhi); });
+}
+int lesgo_gpu_get_field(lesgo_handle_t* h, int f, double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->get_field(f, host, lbz, nzhi); });
+}
+int lesgo_gpu_bind_field(lesgo_handle_t* h, int f, double* host, int lbz, int nzhi) {
+  if (!h || !h->s || !host || f < 0 || f >= LESGO_NFIELDS) return LESGO_ERR_ARG;
+  if (lbz < 0 || nzhi > h->s->der().nz || nzhi < lbz) return LESGO_ERR_ARG;
+  h->bind[f].ptr = host; h->bind[f].lbz = lbz; h->bind[f].nzhi = nzhi;
+  return LESGO_OK;
+}
+int lesgo_gpu_upload(lesgo_handle_t* h, int f) {
+  if (!h || f < 0 || f >= LESGO_NFIELDS || !h->bind[f].ptr) return LESGO_ERR_ARG;
+  return lesgo_gpu_set_field(h, f, h->bind[f].ptr, h->bind[f].lbz, h->bind[f].nzhi);
+}
+int lesgo_gpu_download(lesgo_handle_t* h, int f) {
+  if (!h || f < 0 || f >= LESGO_NFIELDS || !h->bind[f].ptr) return LESGO_ERR_ARG;
+  return lesgo_gpu_get_field(h, f, h->bind[f].ptr, h->bind[f].lbz, h->bind[f].nzhi);
+}
+int lesgo_gpu_init_ic(lesgo_handle_t* h, uint64_t seed) { return guarded(h, [&] { h->s->init_ic(seed); }); }
+
+static bool fid_ok(int f) { return f >= 0 && f < LESGO_NFIELDS; }
+
+int lesgo_gpu_filt_da(lesgo_handle_t* h, int f, int dfdx, int dfdy) {
+  if (!fid_ok(f) || !fid_ok(dfdx) || !fid_ok(dfdy)) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->filt_da(f, dfdx, dfdy); });
+}
+int lesgo_gpu_ddx(lesgo_handle_t* h, int f, int dfdx) {
+  if (!fid_ok(f) || !fid_ok(dfdx)) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->ddxy(f, dfdx, -1); });
+}
+int lesgo_gpu_ddy(lesgo_handle_t* h, int f, int dfdy) {
+  if (!fid_ok(f) || !fid_ok(dfdy)) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->ddxy(f, -1, dfdy); });
+}
+int lesgo_gpu_ddxy(lesgo_handle_t* h, int f, int dfdx, int dfdy) {
+  if (!fid_ok(f) || !fid_ok(dfdx) || !fid_ok(dfdy)) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->ddxy(f, dfdx, dfdy); });
+}
+int lesgo_gpu_ddz_uv(lesgo_handle_t* h, int f, int dfdz) {
+  if (!fid_ok(f) || !fid_ok(dfdz)) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->ddz(f, dfdz, true); });
+}
+int lesgo_gpu_ddz_w(lesgo_handle_t* h, int f, int dfdz) {
+  if (!fid_ok(f) || !fid_ok(dfdz)) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->ddz(f, dfdz, false); });
+}
+int lesgo_gpu_test_filter(lesgo_handle_t* h, int f, int level) {
+  if (!fid_ok(f)) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->test_filter(f, level); });
+}
+int lesgo_gpu_wallstress(lesgo_handle_t* h) { return guarded(h, [&] { h->s->wallstress(); }); }
+int lesgo_gpu_sgs_stag(lesgo_handle_t* h) { return guarded(h, [&] { h->s->sgs_stag(); }); }
+int lesgo_gpu_divstress_uv(lesgo_handle_t* h) { return guarded(h, [&] { h->s->divstress(1); }); }
+int lesgo_gpu_divstress_w(lesgo_handle_t* h) { return guarded(h, [&] { h->s->divstress(2); }); }
+int lesgo_gpu_convec(lesgo_handle_t* h) { return guarded(h, [&] { h->s->convec(); }); }
+int lesgo_gpu_turbines_forcing(lesgo_handle_t* h) { return guarded(h, [&] { h->s->turbines_forcing(); }); }
+int lesgo_gpu_begin_step(lesgo_handle_t* h) { return guarded(h, [&] { h->s->begin_step(); }); }
+int lesgo_gpu_rhs_assemble(lesgo_handle_t* h) { return guarded(h, [&] { h->s->rhs_assemble(); }); }
+int lesgo_gpu_ab2(lesgo_handle_t* h) { return guarded(h, [&] { h->s->ab2(); }); }
+int lesgo_gpu_press_stag_array(lesgo_handle_t* h) { return guarded(h, [&] { h->s->press_stag_array(); }); }
+int lesgo_gpu_rhs_sub_dp(lesgo_handle_t* h) { return guarded(h, [&] { h->s->rhs_sub_dp(); }); }
+int lesgo_gpu_project(lesgo_handle_t* h) { return guarded(h, [&] { h->s->project(); }); }
+int lesgo_gpu_step(lesgo_handle_t* h, int nsteps) {
+  if (nsteps < 0) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->step(nsteps); });
+}
+int lesgo_gpu_sync(lesgo_handle_t* h) {
+  int rc = LESGO_OK;
+  int g = guarded(h, [&] { rc = h->s->sync(); });
+  if (g != LESGO_OK) return g;
+  if (rc != LESGO_OK) h->err = "tridag_array: zero pivot";
+  return rc;
+}
+int lesgo_gpu_diag(lesgo_handle_t* h, double* rmsdiv, double* ke, double* cfl, double* tau_bot) {
+  double out[4] = {0, 0, 0, 0};
+  int rc = guarded(h, [&] { h->s->diag(out); });
+  if (rc == LESGO_OK) {
+    if (rmsdiv) *rmsdiv = out[0];
+    if (ke) *ke = out[1];
+    if (cfl) *cfl = out[2];
+    if (tau_bot) *tau_bot = out[3];
+  }
+  return rc;
+}
+int lesgo_gpu_counters(const lesgo_handle_t* h, int* jt, int* jt_total) {
+  if (!h || !h->s) return LESGO_ERR_ARG;
+  h->s->counters(jt, jt_total);
+  return LESGO_OK;
+}
+int lesgo_gpu_turbine_state(lesgo_handle_t* h, double* u_d_T, double* f_n, double* power, int n) {
+  if (n < 0) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->turbine_state(u_d_T, f_n, power, n); });
+}
+int lesgo_gpu_launches_per_step(const lesgo_handle_t* h, int with_sgs_update) {
+  if (!h || !h->s) return -1;
+  return h->s->launches_per_step(with_sgs_update);
+}
+
+}  // extern "C"

@@ -1,0 +1,235 @@
+"""Host-side mirror of LESGO's time-step subroutines over the C ABI.
+
+``LesgoGPU`` exposes one method per reference subroutine on the hot path
+(``filt_da``, ``ddx``, ``ddz_uv``, ``wallstress``, ``sgs_stag``,
+``divstress_uv``, ``convec``, ``press_stag_array``, ``project`` ...) with
+the same argument meaning, plus the fused ``step``.  Fields are addressed by
+the reference's names (sim_param.f90 / sgs_param.f90).  Host arrays use the
+shape ``(levels, ny, ld)`` in C order, which is byte-identical to the
+reference's Fortran ``(ld, ny, lbz:nzhi)`` arrays.
+
+Failures raise ``LesgoError`` carrying the library's status code, where the
+reference would print and ``stop`` (messages.f90:228-239).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Iterable, Optional
+
+import numpy as np
+
+from . import _lib as L
+
+
+class LesgoError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lesgo_gpu error {code}: {msg}")
+        self.code = code
+
+
+PARAM_DEFAULTS = dict(
+    nx=64, ny=64, Nz=64, L_x=2.0 * 3.1415926535897932384626433, L_y=3.1415926535897932384626433, L_z=1.0,
+    z_i=1000.0, u_star=0.45, vonk=0.4, zo=1.0e-4, dt=2.0e-4, sgs_model=5, cs_count=5, dyn_init=100,
+    ifilter=1, lbc_mom=2, ubc_mom=0, molec=False, nu_molec=1.14e-5, ubot=0.0, utop=0.0,
+    use_mean_p_force=True, eval_mean_p_force=True, mean_p_force_x=1.0, mean_p_force_y=0.0,
+    initu=False, precision="fp64", alpha1=1.5, alpha2=1.5, filter_cutoff=1e-2, T_avg_dim=-1.0,
+    adm_correction=True,
+)
+
+
+class LesgoGPU:
+    """One LES instance resident on the current CUDA device."""
+
+    def __init__(self, turbines: Optional[Iterable[dict]] = None, **kw):
+        unknown = set(kw) - set(PARAM_DEFAULTS)
+        if unknown:
+            raise TypeError(f"unknown parameters: {sorted(unknown)}")
+        cfg = dict(PARAM_DEFAULTS, **kw)
+        self.cfg = cfg
+        self._lib = L.load()
+        p = L.Params()
+        p.nx, p.ny, p.nz_tot = cfg["nx"], cfg["ny"], cfg["Nz"]
+        for name in ("L_x", "L_y", "L_z", "z_i", "u_star", "vonk", "zo", "dt", "nu_molec", "ubot", "utop",
+                     "mean_p_force_x", "mean_p_force_y", "alpha1", "alpha2", "filter_cutoff", "T_avg_dim"):
+            setattr(p, name, float(cfg[name]))
+        for name in ("sgs_model", "cs_count", "dyn_init", "ifilter", "lbc_mom", "ubc_mom"):
+            setattr(p, name, int(cfg[name]))
+        for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction"):
+            setattr(p, name, 1 if cfg[name] else 0)
+        prec = cfg["precision"]
+        p.precision = {"fp64": L.LESGO_FP64, "mixed": L.LESGO_MIXED}[prec] if isinstance(prec, str) else int(prec)
+        tl = list(turbines or [])
+        self._turb = (L.Turbine * max(1, len(tl)))()
+        for i, t in enumerate(tl):
+            for k in ("xloc", "yloc", "height", "dia", "thk", "theta1", "theta2", "Ct_prime"):
+                setattr(self._turb[i], k, float(t.get(k, 0.0 if k.startswith("theta") else 1.33 if k == "Ct_prime" else 0.0)))
+        p.n_turbines = len(tl)
+        p.turbines = C.cast(self._turb, C.POINTER(L.Turbine)) if tl else None
+        self.n_turbines = len(tl)
+        h = C.c_void_p()
+        rc = self._lib.lesgo_gpu_create(C.byref(p), C.byref(h))
+        if rc != L.LESGO_OK:
+            raise LesgoError(rc, self._lib.lesgo_gpu_last_error(None).decode())
+        self._h = h
+        nz, ld, lh, nx2, ny2 = (C.c_int() for _ in range(5))
+        self._lib.lesgo_gpu_dims(h, C.byref(nz), C.byref(ld), C.byref(lh), C.byref(nx2), C.byref(ny2))
+        self.nx, self.ny = cfg["nx"], cfg["ny"]
+        self.nz, self.ld, self.lh, self.nx2, self.ny2 = nz.value, ld.value, lh.value, nx2.value, ny2.value
+
+    # ---------------- lifetime -------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lesgo_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != L.LESGO_OK:
+            raise LesgoError(rc, self._lib.lesgo_gpu_last_error(self._h).decode())
+
+    @staticmethod
+    def _fid(name) -> int:
+        return name if isinstance(name, int) else L.FIELD[name]
+
+    # ---------------- field access ----------------------------------------------
+    def get(self, name, lbz: int = 0, nzhi: Optional[int] = None) -> np.ndarray:
+        nzhi = self.nz if nzhi is None else nzhi
+        out = np.empty((nzhi - lbz + 1, self.ny, self.ld), dtype=np.float64)
+        self._check(self._lib.lesgo_gpu_get_field(self._h, self._fid(name), out.ctypes.data, lbz, nzhi))
+        return out
+
+    def set(self, name, arr: np.ndarray, lbz: int = 0):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if a.ndim != 3 or a.shape[1:] != (self.ny, self.ld):
+            raise ValueError(f"expected (levels, {self.ny}, {self.ld}), got {a.shape}")
+        self._check(self._lib.lesgo_gpu_set_field(self._h, self._fid(name), a.ctypes.data, lbz, lbz + a.shape[0] - 1))
+
+    def set_ptr(self, name, ptr: int, lbz: int, nzhi: int):
+        """Copy levels lbz..nzhi from a host FP64 buffer at address ``ptr``."""
+        self._check(self._lib.lesgo_gpu_set_field(self._h, self._fid(name), C.c_void_p(ptr), lbz, nzhi))
+
+    def get_ptr(self, name, ptr: int, lbz: int, nzhi: int):
+        self._check(self._lib.lesgo_gpu_get_field(self._h, self._fid(name), C.c_void_p(ptr), lbz, nzhi))
+
+    def init_ic(self, seed: int):
+        self._check(self._lib.lesgo_gpu_init_ic(self._h, C.c_uint64(seed)))
+
+    # ---------------- reference subroutines ---------------------------------------
+    def filt_da(self, f, dfdx, dfdy):
+        self._check(self._lib.lesgo_gpu_filt_da(self._h, self._fid(f), self._fid(dfdx), self._fid(dfdy)))
+
+    def ddx(self, f, dfdx):
+        self._check(self._lib.lesgo_gpu_ddx(self._h, self._fid(f), self._fid(dfdx)))
+
+    def ddy(self, f, dfdy):
+        self._check(self._lib.lesgo_gpu_ddy(self._h, self._fid(f), self._fid(dfdy)))
+
+    def ddxy(self, f, dfdx, dfdy):
+        self._check(self._lib.lesgo_gpu_ddxy(self._h, self._fid(f), self._fid(dfdx), self._fid(dfdy)))
+
+    def ddz_uv(self, f, dfdz):
+        self._check(self._lib.lesgo_gpu_ddz_uv(self._h, self._fid(f), self._fid(dfdz)))
+
+    def ddz_w(self, f, dfdz):
+        self._check(self._lib.lesgo_gpu_ddz_w(self._h, self._fid(f), self._fid(dfdz)))
+
+    def test_filter(self, f, level: int):
+        self._check(self._lib.lesgo_gpu_test_filter(self._h, self._fid(f), level))
+
+    def wallstress(self):
+        self._check(self._lib.lesgo_gpu_wallstress(self._h))
+
+    def sgs_stag(self):
+        self._check(self._lib.lesgo_gpu_sgs_stag(self._h))
+
+    def divstress_uv(self):
+        self._check(self._lib.lesgo_gpu_divstress_uv(self._h))
+
+    def divstress_w(self):
+        self._check(self._lib.lesgo_gpu_divstress_w(self._h))
+
+    def convec(self):
+        self._check(self._lib.lesgo_gpu_convec(self._h))
+
+    def turbines_forcing(self):
+        self._check(self._lib.lesgo_gpu_turbines_forcing(self._h))
+
+    def begin_step(self):
+        self._check(self._lib.lesgo_gpu_begin_step(self._h))
+
+    def rhs_assemble(self):
+        self._check(self._lib.lesgo_gpu_rhs_assemble(self._h))
+
+    def ab2(self):
+        self._check(self._lib.lesgo_gpu_ab2(self._h))
+
+    def press_stag_array(self):
+        self._check(self._lib.lesgo_gpu_press_stag_array(self._h))
+
+    def rhs_sub_dp(self):
+        self._check(self._lib.lesgo_gpu_rhs_sub_dp(self._h))
+
+    def project(self):
+        self._check(self._lib.lesgo_gpu_project(self._h))
+
+    def step_reference_order(self):
+        """One time step through the stand-alone entry points in the order
+        of main.f90:130-344 (the drop-in call sequence)."""
+        self.begin_step()
+        self.filt_da("u", "dudx", "dudy")
+        self.filt_da("v", "dvdx", "dvdy")
+        self.filt_da("w", "dwdx", "dwdy")
+        self.ddz_uv("u", "dudz")
+        self.ddz_uv("v", "dvdz")
+        self.ddz_w("w", "dwdz")
+        self.wallstress()
+        self.sgs_stag()
+        self.divstress_uv()
+        self.divstress_w()
+        self.convec()
+        if self.n_turbines:
+            self.turbines_forcing()
+        self.rhs_assemble()
+        self.ab2()
+        self.press_stag_array()
+        self.rhs_sub_dp()
+        self.project()
+
+    # ---------------- fused loop, diagnostics ----------------------------------------
+    def step(self, nsteps: int = 1):
+        self._check(self._lib.lesgo_gpu_step(self._h, nsteps))
+
+    def sync(self):
+        self._check(self._lib.lesgo_gpu_sync(self._h))
+
+    def diag(self) -> Dict[str, float]:
+        r, k, c, t = (C.c_double() for _ in range(4))
+        self._check(self._lib.lesgo_gpu_diag(self._h, C.byref(r), C.byref(k), C.byref(c), C.byref(t)))
+        return dict(rmsdiv=r.value, ke=k.value, cfl=c.value, tau_bot=t.value)
+
+    def counters(self):
+        a, b = C.c_int(), C.c_int()
+        self._check(self._lib.lesgo_gpu_counters(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def turbine_state(self):
+        n = self.n_turbines
+        a, b, c = (np.zeros(max(n, 1)) for _ in range(3))
+        dp = C.POINTER(C.c_double)
+        self._check(self._lib.lesgo_gpu_turbine_state(self._h, a.ctypes.data_as(dp), b.ctypes.data_as(dp),
+                                                      c.ctypes.data_as(dp), n))
+        return dict(u_d_T=a[:n], f_n=b[:n], power=c[:n])
+
+    def launches_per_step(self, with_sgs_update: bool = False) -> int:
+        return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
