@@ -193,6 +193,16 @@ int lesgo_gpu_turbine_state(lesgo_handle_t* h, double* u_d_T, double* f_n, doubl
  * given kind (0: normal step, 1: step with the dynamic SGS update). */
 int lesgo_gpu_launches_per_step(const lesgo_handle_t* h, int with_sgs_update);
 
+/* ---- instrumentation (no reference counterpart; the reference only
+ * prints wall-clock times, main.f90:359-436) --------------------------- */
+/* enable != 0: run steps eagerly (no graph replay) with a CUDA event pair
+ * on the handle's stream around every kernel; resets the records. */
+int lesgo_gpu_profile(lesgo_handle_t* h, int enable);
+/* JSON object {"kernel": [launches, total_ms, algorithmic_bytes], ...}. */
+int lesgo_gpu_profile_report(lesgo_handle_t* h, char* buf, int buflen);
+/* The cudaStream_t the handle launches on (for events recorded by callers). */
+int lesgo_gpu_get_stream(const lesgo_handle_t* h, void** stream);
+
 #ifdef __cplusplus
 }
 #endif

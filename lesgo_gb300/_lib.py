@@ -92,6 +92,9 @@ SIGNATURES = {
     "lesgo_gpu_counters": (_I, [_H, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_turbine_state": (_I, [_H, _D, _D, _D, _I]),
     "lesgo_gpu_launches_per_step": (_I, [_H, _I]),
+    "lesgo_gpu_profile": (_I, [_H, _I]),
+    "lesgo_gpu_profile_report": (_I, [_H, C.c_char_p, _I]),
+    "lesgo_gpu_get_stream": (_I, [_H, C.POINTER(C.c_void_p)]),
 }
 
 _lib = None

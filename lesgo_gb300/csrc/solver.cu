@@ -318,6 +318,9 @@ class SolverBase {
   virtual void counters(int* jt, int* jt_total) const = 0;
   virtual void turbine_state(double* udT, double* fn, double* pw, int n) = 0;
   virtual int launches_per_step(int with_sgs) const = 0;
+  virtual void profile(int enable) = 0;
+  virtual std::string profile_report() = 0;
+  virtual void* stream() const = 0;
 };
 
 template <typename R>
@@ -364,6 +367,7 @@ class Solver : public SolverBase {
   }
 
   ~Solver() override {
+    for (auto& r : prof_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
     for (void* p : allocs_) cudaFree(p);
     if (st_) cudaStreamDestroy(st_);
@@ -471,12 +475,13 @@ class Solver : public SolverBase {
     const R idz = (R)(1.0 / d_.dz);
     if (which == 3) {
       SrcFields<R, 5> src{{F_[LESGO_TXX], F_[LESGO_TXY], F_[LESGO_TYY], F_[LESGO_TXZ], F_[LESGO_TYZ]}, sc, 1, 1, d_.ld, kp_.plane};
-      xfwd<5>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+      xfwd<5>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_, "divstress.xfwd");
       ypass_lin<5, 3, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
-                                          {{MUL_IKX, MUL_IKY, 0, 0, 0}, {0, MUL_IKX, MUL_IKY, 0, 0}, {0, 0, 0, MUL_IKX, MUL_IKY}});
+                                          {{MUL_IKX, MUL_IKY, 0, 0, 0}, {0, MUL_IKX, MUL_IKY, 0, 0}, {0, 0, 0, MUL_IKX, MUL_IKY}},
+                                          "divstress.ypass");
       DstDiv<R, 3> dst{F_[LESGO_DIVTX], F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_TZZ],
                        idz, d_.ld, d_.nz, kp_.plane};
-      xinv<3>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+      xinv<3>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_, "divstress.xinv", 6);
     } else if (which == 1) {
       SrcFields<R, 3> src{{F_[LESGO_TXX], F_[LESGO_TXY], F_[LESGO_TYY]}, sc, 1, 1, d_.ld, kp_.plane};
       xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
@@ -630,6 +635,39 @@ class Solver : public SolverBase {
     }
   }
 
+  // Profiling: eager steps with an event pair per launch; the report is a
+  // JSON object {name: [launches, total_ms, total_bytes]}.
+  void profile(int enable) override {
+    CK(cudaStreamSynchronize(st_));
+    for (auto& r : prof_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    prof_.clear();
+    prof_on_ = enable != 0;
+    use_graphs_ = !prof_on_;
+  }
+  std::string profile_report() override {
+    CK(cudaStreamSynchronize(st_));
+    std::map<std::string, std::tuple<long long, double, double>> agg;
+    for (auto& r : prof_) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, r.a, r.b));
+      auto& t = agg[r.name];
+      std::get<0>(t) += 1;
+      std::get<1>(t) += ms;
+      std::get<2>(t) += r.bytes;
+    }
+    std::string out = "{";
+    bool first = true;
+    for (auto& kv : agg) {
+      char buf[512];
+      std::snprintf(buf, sizeof(buf), "%s\"%s\": [%lld, %.6f, %.1f]", first ? "" : ", ", kv.first.c_str(),
+                    std::get<0>(kv.second), std::get<1>(kv.second), std::get<2>(kv.second));
+      out += buf;
+      first = false;
+    }
+    return out + "}";
+  }
+  void* stream() const override { return (void*)st_; }
+
   int launches_per_step(int with_sgs) const override {
     for (auto& kv : launch_count_) {
       StepKey k = StepKey::from(kv.first);
@@ -652,12 +690,12 @@ class Solver : public SolverBase {
   void step_body(const StepKey& key) {
     // main.f90:155-172: derivatives (RHS_f is saved inside the fused convec epilogue)
     SrcFields<R, 3> src{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, (R)(1.0 / ((double)d_.nx * d_.ny)), 1, 1, d_.ld, kp_.plane};
-    xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+    xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_, "filt_da.xfwd");
     ypass_lin<1, 3, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 3, ROW_SAME,
-                                        {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}});
+                                        {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}}, "filt_da.ypass");
     DstFields<R, 9> dst{{F_[LESGO_U], F_[LESGO_DUDX], F_[LESGO_DUDY], F_[LESGO_V], F_[LESGO_DVDX], F_[LESGO_DVDY],
                          F_[LESGO_W], F_[LESGO_DWDX], F_[LESGO_DWDY]}, 1, 1, d_.ld, kp_.plane};
-    xinv<9>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    xinv<9>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_, "filt_da.xinv");
     // wall model inputs (test-filtered first level), main.f90:180-189
     wall_planes();
     // applied forcing uses the filtered velocity of this step (main.f90:248-257)
@@ -692,11 +730,31 @@ class Solver : public SolverBase {
     return staging_;
   }
   static dim3 grid1(long long n) { return dim3((unsigned)((n + 255) / 256)); }
-  void post() {
+  // Every launch is bracketed by pre() / post(name, bytes).  With profiling
+  // on (eager steps only) an event pair on the handle's stream times it;
+  // `bytes` is the launch's algorithmic traffic (unique inputs + outputs at
+  // storage precision).
+  void pre() {
+    if (prof_on_) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      CK(cudaEventRecord(e, st_));
+      prof_start_ = e;
+    }
+  }
+  void post(const char* name = "aux", double bytes = 0.0) {
     ++launches_;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw Error(LESGO_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    if (prof_on_ && prof_start_) {
+      cudaEvent_t e1;
+      CK(cudaEventCreate(&e1));
+      CK(cudaEventRecord(e1, st_));
+      prof_.push_back(ProfRec{name, bytes, prof_start_, e1});
+      prof_start_ = nullptr;
+    }
   }
+  struct ProfRec { std::string name; double bytes; cudaEvent_t a, b; };
   template <typename KF>
   static void set_smem(KF kern, size_t bytes) {
     if (bytes > 48 * 1024) {
@@ -810,7 +868,8 @@ class Solver : public SolverBase {
   }
 
   template <int NF, class Src>
-  void xfwd(const Src& src, int M, int nyrows, int nlev, T2* out, long long out_fs, const FftPlan<R>& plan) {
+  void xfwd(const Src& src, int M, int nyrows, int nlev, T2* out, long long out_fs, const FftPlan<R>& plan,
+            const char* tag = "xfwd", int in_fields = NF) {
     XfGeom g;
     g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nlev; g.ls = M / 2 + 1;
     const int target = sizeof(R) == 8 ? 2048 : 4096;
@@ -819,12 +878,14 @@ class Solver : public SolverBase {
     const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
     auto kern = k_xfwd<R, NF, Src>;
     set_smem(kern, smem);
+    pre();
     kern<<<(g.nrows + g.rpc - 1) / g.rpc, 256, smem, st_>>>(g, plan, src, out);
-    post();
+    post(tag, (double)g.nrows * ((double)in_fields * M * sizeof(R) + (double)NF * g.K * sizeof(T2)));
   }
 
   template <int NF, class Dst>
-  void xinv(const Dst& dst, const T2* in, long long in_fs, int M, int nyrows, int nlev, const FftPlan<R>& plan) {
+  void xinv(const Dst& dst, const T2* in, long long in_fs, int M, int nyrows, int nlev, const FftPlan<R>& plan,
+            const char* tag = "xinv", int out_fields = NF) {
     XiGeom g;
     g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nlev; g.ls = M / 2 + 1;
     const int target = sizeof(R) == 8 ? 2048 : 4096;
@@ -833,14 +894,16 @@ class Solver : public SolverBase {
     const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
     auto kern = k_xinv<R, NF, Dst>;
     set_smem(kern, smem);
+    pre();
     kern<<<(g.nrows + g.rpc - 1) / g.rpc, 256, smem, st_>>>(g, plan, in, dst);
-    post();
+    post(tag, (double)g.nrows * ((double)NF * g.K * sizeof(T2) + (double)out_fields * M * sizeof(R)));
   }
 
   // Y pass over groups of NIN inputs -> NOUT outputs.
   template <int NIN, int NOUT, bool FWD, bool INV, typename InT, typename OutT>
   void ypass_lin(const InT* in, long long in_fs, int in_lev0, int in_levstride, int in_rows, OutT* out, long long out_fs,
-                 int out_rows, int nlev, int ngroups, int rowmode, std::initializer_list<std::initializer_list<int>> mul) {
+                 int out_rows, int nlev, int ngroups, int rowmode, std::initializer_list<std::initializer_list<int>> mul,
+                 const char* tag = "ypass") {
     YOpLin<R, NIN, NOUT, InT, OutT> op;
     op.in = in; op.in_fs = in_fs; op.in_lev0 = in_lev0; op.in_levstride = in_levstride; op.in_rows = in_rows;
     op.out = out; op.out_fs = out_fs; op.out_rows = out_rows;
@@ -872,22 +935,24 @@ class Solver : public SolverBase {
     auto kern = k_ypass<R, NIN, NOUT, FWD, INV, YOpLin<R, NIN, NOUT, InT, OutT>>;
     set_smem(kern, smem);
     dim3 grid((d_.K + tk - 1) / tk, nlev, ngroups);
+    pre();
     kern<<<grid, 256, smem, st_>>>(g, pin, pout, op);
-    post();
+    post(tag, (double)ngroups * nlev * d_.K *
+                  ((double)NIN * in_rows * sizeof(InT) + (double)NOUT * out_rows * sizeof(OutT)));
   }
 
   // test-filter (G_test) of one plane of two fields into two (ld, ny) planes
   void filter_planes(const R* a, const R* b, int level, R* oa, R* ob, int nf) {
     SrcFields<R, 2> src{{a, b}, (R)1, level, 1, d_.ld, kp_.plane};
-    xfwd<2>(src, d_.nx, d_.ny, 1, specC_, (long long)d_.ny * d_.K, px_);
+    xfwd<2>(src, d_.nx, d_.ny, 1, specC_, (long long)d_.ny * d_.K, px_, "wall_filter.xfwd");
     ypass_lin<1, 1, true, true, T2, T2>(specC_, (long long)d_.ny * d_.K, 0, 1, d_.ny, specC_ + 2LL * d_.ny * d_.K,
-                                        (long long)d_.ny * d_.K, d_.ny, 1, 2, ROW_SAME, {{MUL_G1}});
+                                        (long long)d_.ny * d_.K, d_.ny, 1, 2, ROW_SAME, {{MUL_G1}}, "wall_filter.ypass");
     if (nf == 1) {
       DstFields<R, 1> dst{{oa}, 0, 1, d_.ld, 0};
-      xinv<1>(dst, specC_ + 2LL * d_.ny * d_.K, (long long)d_.ny * d_.K, d_.nx, d_.ny, 1, px_);
+      xinv<1>(dst, specC_ + 2LL * d_.ny * d_.K, (long long)d_.ny * d_.K, d_.nx, d_.ny, 1, px_, "wall_filter.xinv");
     } else {
       DstFields<R, 2> dst{{oa, ob}, 0, 1, d_.ld, 0};
-      xinv<2>(dst, specC_ + 2LL * d_.ny * d_.K, (long long)d_.ny * d_.K, d_.nx, d_.ny, 1, px_);
+      xinv<2>(dst, specC_ + 2LL * d_.ny * d_.K, (long long)d_.ny * d_.K, d_.nx, d_.ny, 1, px_, "wall_filter.xinv");
     }
   }
   void wall_planes() {
@@ -914,8 +979,11 @@ class Solver : public SolverBase {
     a.cs_fill = cs_fill ? 1 : 0;
     const int ncol = d_.nx * d_.ny;
     dim3 grid((ncol + 255) / 256, (d_.nz + a.chunk - 1) / a.chunk);
+    const int nrw = (FLAGS & COL_READ_S) ? 13 : (FLAGS & COL_TAU) ? 19 : 18;
+    pre();
     k_column<R, FLAGS><<<grid, 256, 0, st_>>>(a);
-    post();
+    post((FLAGS & COL_READ_S) ? "sgs_column.tau" : (FLAGS & COL_TAU) ? "sgs_column" : "sgs_column.sij",
+         (double)nrw * ncol * d_.nz * sizeof(R));
     if (cs_fill && !(FLAGS & COL_TAU)) {
       k_fill<R><<<grid1(nfield_), 256, 0, st_>>>(F_[LESGO_CS_OPT2], nfield_, (R)0.03);
       post();
@@ -929,13 +997,14 @@ class Solver : public SolverBase {
     for (int f = 0; f < 4; ++f) { ia.Fin[f] = F_[Fi[f]]; ia.Fout[f] = Ftmp_[f]; }
     ia.kp = kp_;
     const long long n = (long long)d_.nx * d_.ny * d_.nz;
+    pre();
     k_interp<R><<<grid1(n), 256, 0, st_>>>(ia);
-    post();
+    post("lagrange.interp", 11.0 * n * sizeof(R));
     SrcLagrange<R> src{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_S11], F_[LESGO_S12], F_[LESGO_S13],
                        F_[LESGO_S22], F_[LESGO_S23], F_[LESGO_S33], d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane};
-    xfwd<21>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+    xfwd<21>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_, "lagrange.xfwd", 9);
     ypass_lin<1, 2, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 21, ROW_SAME,
-                                        {{MUL_G1}, {MUL_G2}});
+                                        {{MUL_G1}, {MUL_G2}}, "lagrange.ypass");
     DstLagrange<R> dst;
     dst.FLMi = Ftmp_[0]; dst.FMMi = Ftmp_[1]; dst.FQNi = Ftmp_[2]; dst.FNNi = Ftmp_[3];
     dst.FLM = F_[LESGO_F_LM]; dst.FMM = F_[LESGO_F_MM]; dst.FQN = F_[LESGO_F_QN]; dst.FNN = F_[LESGO_F_NN];
@@ -947,7 +1016,7 @@ class Solver : public SolverBase {
     dst.ld = d_.ld; dst.nz = d_.nz; dst.lbc = kp_.lbc; dst.ubc = kp_.ubc;
     dst.init_lm = init_lm; dst.init_qn = init_qn;
     dst.plane = kp_.plane;
-    xinv<42>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    xinv<42>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_, "lagrange.xinv", 13);
   }
   void lagrange() {
     const bool inilag = !d_.p.initu;
@@ -962,14 +1031,16 @@ class Solver : public SolverBase {
     const R c = (R)(1.0 / ((double)d_.nx * d_.ny));
     SrcVort<R> sv{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDY], F_[LESGO_DUDZ], F_[LESGO_DVDX],
                   F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane};
-    xfwd<6>(sv, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
-    ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_b_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}});
+    xfwd<6>(sv, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_, "convec.xfwd", 9);
+    ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_b_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}},
+                                        "convec.ypass_pad");
     DstFields<R, 6> db{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld_big, kp_.plane_big};
-    xinv<6>(db, specB_, vol_b_, d_.nx2, d_.ny2, d_.nz, pxb_);
+    xinv<6>(db, specB_, vol_b_, d_.nx2, d_.ny2, d_.nz, pxb_, "convec.xinv_big");
     const R cb = (R)(1.0 / ((double)d_.nx2 * d_.ny2));
     SrcConvProd<R> sp{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5], cb, d_.ld_big, d_.nz, kp_.plane_big};
-    xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, specA_, vol_b_, pxb_);
-    ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_b_, 0, 1, d_.ny2, specB_, vol_s_, d_.ny, d_.nz, 3, ROW_UNPAD, {{MUL_ONE}});
+    xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, specA_, vol_b_, pxb_, "convec.xfwd_big", 6);
+    ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_b_, 0, 1, d_.ny2, specB_, vol_s_, d_.ny, d_.nz, 3, ROW_UNPAD, {{MUL_ONE}},
+                                        "convec.ypass_unpad");
     if (!fused) {
       DstConvec<R, false> dc{};
       dc.RHSx = F_[LESGO_RHSX]; dc.RHSy = F_[LESGO_RHSY]; dc.RHSz = F_[LESGO_RHSZ];
@@ -985,7 +1056,7 @@ class Solver : public SolverBase {
       dc.dt = d_.p.dt; dc.t1 = d_.tadv1; dc.t2 = d_.tadv2; dc.mpfx = d_.mpfx; dc.mpfy = d_.mpfy;
       dc.ld = d_.ld; dc.nz = d_.nz; dc.euler = euler ? 1 : 0; dc.use_mpf = d_.p.use_mean_p_force; dc.turbines = kp_.turbines;
       dc.plane = kp_.plane;
-      xinv<3>(dc, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+      xinv<3>(dc, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_, "convec.xinv_ab2", 18 + 3 * kp_.turbines);
     }
   }
 
@@ -995,53 +1066,61 @@ class Solver : public SolverBase {
     const double c1 = 1.0 / ((double)d_.nx * d_.ny);
     const R c2 = (R)(c1 / d_.tadv1 / d_.p.dt);
     SrcFields<R, 3> su{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, c2, 1, 1, d_.ld, kp_.plane};
-    xfwd<3>(su, d_.nx, ny, nz, specA_, vol_s_, px_);
+    xfwd<3>(su, d_.nx, ny, nz, specA_, vol_s_, px_, "press.xfwd");
     SrcFields<R, 1> sd{{F_[LESGO_DIVTZ]}, (R)c1, 1, nz - 1, d_.ld, kp_.plane};
-    xfwd<1>(sd, d_.nx, ny, 2, specC_, 2 * pl_s, px_);
-    ypass_lin<1, 1, true, false, T2, double2>(specA_, vol_s_, 0, 1, ny, hspec_, vol_s_, ny, nz, 3, ROW_SAME, {{MUL_ONE}});
-    ypass_lin<1, 1, true, false, T2, double2>(specC_, 2 * pl_s, 0, 1, ny, hplane_, 2 * pl_s, ny, 2, 1, ROW_SAME, {{MUL_ONE}});
+    xfwd<1>(sd, d_.nx, ny, 2, specC_, 2 * pl_s, px_, "press.xfwd_bc");
+    ypass_lin<1, 1, true, false, T2, double2>(specA_, vol_s_, 0, 1, ny, hspec_, vol_s_, ny, nz, 3, ROW_SAME, {{MUL_ONE}},
+                                              "press.ypass_fwd");
+    ypass_lin<1, 1, true, false, T2, double2>(specC_, 2 * pl_s, 0, 1, ny, hplane_, 2 * pl_s, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
+                                              "press.ypass_fwd_bc");
     ThomasArgs ta;
     ta.Hx = hspec_; ta.Hy = hspec_ + vol_s_; ta.Hz = hspec_ + 2 * vol_s_;
     ta.Hb = hplane_; ta.Ht = hplane_ + pl_s;
     ta.phat = phat_; ta.gam = gam_;
     ta.kxw = kxw64_; ta.kyw = kyw64_;
     ta.dz = d_.dz; ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.err = err_;
+    pre();
     k_thomas<<<(unsigned)((pl_s + 127) / 128), 128, 0, st_>>>(ta);
-    post();
+    post("press.thomas", (double)pl_s * (4.0 * nz + 1.0) * sizeof(double2));
     // p, i kx p, i ky p at levels 1..nz-1; p at levels 0 and nz
     ypass_lin<1, 3, false, true, double2, T2>(phat_, 0, 1, 1, ny, specB_, vol_s_, ny, nz - 1, 1, ROW_SAME,
-                                              {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}});
-    ypass_lin<1, 1, false, true, double2, T2>(phat_, 0, 0, nz, ny, specC_, 2 * pl_s, ny, 2, 1, ROW_SAME, {{MUL_ONE}});
+                                              {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}}, "press.ypass_inv");
+    ypass_lin<1, 1, false, true, double2, T2>(phat_, 0, 0, nz, ny, specC_, 2 * pl_s, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
+                                              "press.ypass_inv_bc");
     if (fused) {
       DstPress<R, true> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U], F_[LESGO_V],
                            d_.p.dt, d_.tadv1, d_.ld, kp_.plane};
-      xinv<3>(dp, specB_, vol_s_, d_.nx, ny, nz - 1, px_);
+      xinv<3>(dp, specB_, vol_s_, d_.nx, ny, nz - 1, px_, "press.xinv_project", 9);
     } else {
       DstPress<R, false> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U], F_[LESGO_V],
                             d_.p.dt, d_.tadv1, d_.ld, kp_.plane};
       xinv<3>(dp, specB_, vol_s_, d_.nx, ny, nz - 1, px_);
     }
     DstFields<R, 1> d0{{F_[LESGO_P]}, 0, nz, d_.ld, kp_.plane};
-    xinv<1>(d0, specC_, 2 * pl_s, d_.nx, ny, 2, px_);
+    xinv<1>(d0, specC_, 2 * pl_s, d_.nx, ny, 2, px_, "press.xinv_bc");
     const long long n = (long long)d_.nx * ny * nz;
+    pre();
     if (fused)
       k_wproj<R, true><<<grid1(n), 256, 0, st_>>>(F_[LESGO_P], F_[LESGO_DPDZ], F_[LESGO_RHSZ], F_[LESGO_U], F_[LESGO_V],
                                                   F_[LESGO_W], kp_);
     else
       k_wproj<R, false><<<grid1(n), 256, 0, st_>>>(F_[LESGO_P], F_[LESGO_DPDZ], F_[LESGO_RHSZ], F_[LESGO_U], F_[LESGO_V],
                                                    F_[LESGO_W], kp_);
-    post();
+    post("press.wproj", (fused ? 5.0 : 2.0) * n * sizeof(R));
   }
 
   void turb_impl() {
+    pre();
     k_turb_disk<R><<<th_.n, 256, 0, st_>>>(td_, F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_.plane, d_.nz);
-    post();
+    post("turbines.disk", (double)th_.node_q.size() * (4 * sizeof(R) + 16.0));
     if (td_.nwin > 0) {
+      pre();
       k_turb_scatter<R><<<(td_.nwin + 255) / 256, 256, 0, st_>>>(td_, F_[LESGO_FXA], F_[LESGO_FYA], fza_uv_);
-      post();
+      post("turbines.scatter", (double)td_.nwin * (3 * sizeof(R) + 20.0));
       const long long n = (long long)th_.cols.size() * d_.nz;
+      pre();
       k_turb_fzw<R><<<grid1(n), 256, 0, st_>>>(fza_uv_, F_[LESGO_FZA], cols_, (int)th_.cols.size(), kp_);
-      post();
+      post("turbines.fzw", 2.0 * n * sizeof(R));
     }
   }
 
@@ -1072,6 +1151,9 @@ class Solver : public SolverBase {
   bool F_LM_MM_init_ = false, F_QN_NN_init_ = false;
   bool use_graphs_ = true;
   int launches_ = 0;
+  bool prof_on_ = false;
+  cudaEvent_t prof_start_ = nullptr;
+  std::vector<ProfRec> prof_;
   std::map<int, cudaGraphExec_t> graphs_;
   std::map<int, int> launch_count_;
 };
@@ -1271,4 +1353,22 @@ int lesgo_gpu_launches_per_step(const lesgo_handle_t* h, int with_sgs_update) {
   return h->s->launches_per_step(with_sgs_update);
 }
 
+}  // extern "C"
+
+extern "C" {
+int lesgo_gpu_profile(lesgo_handle_t* h, int enable) { return guarded(h, [&] { h->s->profile(enable); }); }
+int lesgo_gpu_profile_report(lesgo_handle_t* h, char* buf, int buflen) {
+  if (!buf || buflen <= 0) return LESGO_ERR_ARG;
+  std::string r;
+  int rc = guarded(h, [&] { r = h->s->profile_report(); });
+  if (rc != LESGO_OK) return rc;
+  if ((int)r.size() + 1 > buflen) return LESGO_ERR_ARG;
+  std::memcpy(buf, r.c_str(), r.size() + 1);
+  return LESGO_OK;
+}
+int lesgo_gpu_get_stream(const lesgo_handle_t* h, void** stream) {
+  if (!h || !h->s || !stream) return LESGO_ERR_ARG;
+  *stream = h->s->stream();
+  return LESGO_OK;
+}
 }  // extern "C"

@@ -231,5 +231,19 @@ class LesgoGPU:
                                                       c.ctypes.data_as(dp), n))
         return dict(u_d_T=a[:n], f_n=b[:n], power=c[:n])
 
+    def profile(self, enable: bool = True):
+        self._check(self._lib.lesgo_gpu_profile(self._h, 1 if enable else 0))
+
+    def profile_report(self) -> dict:
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        self._check(self._lib.lesgo_gpu_profile_report(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def stream_ptr(self) -> int:
+        s = C.c_void_p()
+        self._check(self._lib.lesgo_gpu_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
     def launches_per_step(self, with_sgs_update: bool = False) -> int:
         return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
