@@ -982,20 +982,7 @@ class Oracle:
         mask[:, lh - 1] = False
         mask[ny // 2, :] = False
         mask[0, 0] = False
-        cols = np.s_[:, : lh - 1]
-        P = np.zeros((n + 1, ny, lh), dtype=complex)      # P[m] = p level m-1
-        P[1][cols] = r[1][cols] / b[1][cols]
-        bet = b[1].copy()
-        gam = np.zeros((n + 1, ny, lh))
-        for j in range(2, n + 1):
-            g = np.where(mask, c[j - 1] / np.where(mask, bet, 1.0), 0.0)
-            gam[j] = g
-            bet = np.where(mask, b[j] - a[j] * g, bet)
-            if np.any(mask & (bet == 0.0)):
-                raise ZeroDivisionError("tridag_array failed (zero pivot)")
-            P[j] = np.where(mask, (r[j] - a[j] * P[j - 1]) / np.where(mask, bet, 1.0), P[j])
-        for j in range(n - 1, 0, -1):
-            P[j] = np.where(mask, P[j] - gam[j + 1] * P[j + 1], P[j])
+        P = tridag_array(a, b, c, r, mask)
         ph = P[1:]                                         # levels 0..nz
         # zero-wavenumber solution (:226-234)
         ph[0, 0, 0] = 0.0
@@ -1248,6 +1235,35 @@ class Oracle:
     def step(self):
         for _, fn, _ in self.stages():
             fn()
+
+
+def tridag_array(a, b, c, r, mask):
+    """tridag_array.f90:166-246 (serial Thomas algorithm) on all columns.
+
+    a, b, c: real (n+1, ny, lh) with index 1..n used; r: complex, same shape.
+    ``mask`` selects the columns the reference solves (it skips the ky
+    Nyquist row and the kx = ky = 0 column in the sweeps); level 1 is set
+    for every kx < nx/2 column as in the reference.  Returns u (index 1..n).
+    """
+    n = a.shape[0] - 1
+    lh = a.shape[2]
+    cols = np.s_[:, : lh - 1]
+    u = np.zeros(r.shape, dtype=complex)
+    if np.any(b[1][cols] == 0.0):
+        raise ZeroDivisionError("tridag_array: rewrite eqs (b(1) = 0)")
+    u[1][cols] = r[1][cols] / b[1][cols]
+    bet = b[1].copy()
+    gam = np.zeros(a.shape)
+    for j in range(2, n + 1):
+        g = np.where(mask, c[j - 1] / np.where(mask, bet, 1.0), 0.0)
+        gam[j] = g
+        bet = np.where(mask, b[j] - a[j] * g, bet)
+        if np.any(mask & (bet == 0.0)):
+            raise ZeroDivisionError("tridag_array failed (zero pivot)")
+        u[j] = np.where(mask, (r[j] - a[j] * u[j - 1]) / np.where(mask, bet, 1.0), u[j])
+    for j in range(n - 1, 0, -1):
+        u[j] = np.where(mask, u[j] - gam[j + 1] * u[j + 1], u[j])
+    return u
 
 
 def round_half_away(x: float) -> float:
