@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <complex>
 #include <cstring>
 #include <map>
@@ -361,6 +362,9 @@ class Solver : public SolverBase {
     phat_ = alloc<double2>((nz + 1) * pl_s);
     gam_ = alloc<double>((nz + 2) * pl_s);
     err_ = alloc<int>(1);
+    // LESGO_GRAPHS=0 replays nothing: every step launches eagerly
+    if (const char* g = std::getenv("LESGO_GRAPHS")) graphs_allowed_ = std::strcmp(g, "0") != 0;
+    use_graphs_ = graphs_allowed_;
     build_tables();
     if (kp_.turbines) build_turbines();
     CK(cudaStreamSynchronize(st_));
@@ -642,7 +646,7 @@ class Solver : public SolverBase {
     for (auto& r : prof_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     prof_.clear();
     prof_on_ = enable != 0;
-    use_graphs_ = !prof_on_;
+    use_graphs_ = graphs_allowed_ && !prof_on_;
   }
   std::string profile_report() override {
     CK(cudaStreamSynchronize(st_));
@@ -1149,7 +1153,7 @@ class Solver : public SolverBase {
   long long* cols_ = nullptr;
   int jt_ = 0, jt_total_ = 0;
   bool F_LM_MM_init_ = false, F_QN_NN_init_ = false;
-  bool use_graphs_ = true;
+  bool use_graphs_ = true, graphs_allowed_ = true;
   int launches_ = 0;
   bool prof_on_ = false;
   cudaEvent_t prof_start_ = nullptr;
