@@ -167,6 +167,13 @@ int lesgo_gpu_press_stag_array(lesgo_handle_t* h);
 int lesgo_gpu_rhs_sub_dp(lesgo_handle_t* h);
 /* forcing.f90:149-244 */
 int lesgo_gpu_project(lesgo_handle_t* h);
+/* tridag_array.f90:166-246 on device arrays in the reference layout:
+ * a, b, c real (lh, ny, n); r, u interleaved complex (2*lh, ny, n).  Solves
+ * every kx < nx/2 column except the ky Nyquist row and kx = ky = 0 (whose
+ * first level is still set to r/b).  Runs on the handle's stream and
+ * returns when done; LESGO_ERR_NUMERIC on a zero pivot. */
+int lesgo_gpu_tridag_array(lesgo_handle_t* h, const double* a, const double* b, const double* c,
+                           const double* r, double* u, int lh, int ny, int n);
 
 /* ---- fused time loop ---------------------------------------------------- */
 /* Advance nsteps full time steps (main.f90:130-344) with fused kernels and

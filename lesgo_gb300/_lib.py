@@ -86,6 +86,7 @@ SIGNATURES = {
     "lesgo_gpu_press_stag_array": (_I, [_H]),
     "lesgo_gpu_rhs_sub_dp": (_I, [_H]),
     "lesgo_gpu_project": (_I, [_H]),
+    "lesgo_gpu_tridag_array": (_I, [_H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _I, _I, _I]),
     "lesgo_gpu_step": (_I, [_H, _I]),
     "lesgo_gpu_sync": (_I, [_H]),
     "lesgo_gpu_diag": (_I, [_H, _D, _D, _D, _D]),

@@ -729,3 +729,48 @@ __global__ void k_turb_fzw(const R* fza, R* fzw, const long long* cols, int ncol
 }
 
 }  // namespace lesgo
+
+namespace lesgo {
+
+// tridag_array.f90:166-246 on caller arrays in the reference layout:
+// a, b, c real (lh, ny, n); r, u interleaved complex (2*lh, ny, n).  One
+// thread per (kx, ky) column: u(1) = r(1)/b(1) for every kx < nx/2, then
+// the Thomas sweeps skip the ky Nyquist row and the kx = ky = 0 column.
+// `gam` is scratch of lh*ny*n doubles; a zero pivot sets *err.
+__global__ void __launch_bounds__(128) k_tridag(const double* __restrict__ a, const double* __restrict__ b,
+                                                const double* __restrict__ c, const double2* __restrict__ r,
+                                                double2* __restrict__ u, double* __restrict__ gam,
+                                                int lh, int ny, int n, int* err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ncol = (lh - 1) * ny;
+  if (t >= ncol) return;
+  const int jy = t / (lh - 1), jx = t - jy * (lh - 1);
+  const long long col = (long long)jy * lh + jx;
+  const long long L = (long long)lh * ny;     // stride between levels
+  double bet = b[col];
+  if (bet == 0.0) { atomicExch(err, 1); return; }
+  double2 up = make_double2(r[col].x / bet, r[col].y / bet);
+  u[col] = up;
+  if (jy == ny / 2 || (jx == 0 && jy == 0)) return;
+  for (int j = 1; j < n; ++j) {
+    const long long q = j * L + col;
+    const double g = c[q - L] / bet;
+    gam[q] = g;
+    bet = b[q] - a[q] * g;
+    if (bet == 0.0) { atomicExch(err, 1); return; }
+    const double2 rr = r[q];
+    up = make_double2((rr.x - a[q] * up.x) / bet, (rr.y - a[q] * up.y) / bet);
+    u[q] = up;
+  }
+  double2 un = up;
+  for (int j = n - 2; j >= 0; --j) {
+    const long long q = j * L + col;
+    const double g = gam[q + L];
+    double2 uj = u[q];
+    uj = make_double2(uj.x - g * un.x, uj.y - g * un.y);
+    u[q] = uj;
+    un = uj;
+  }
+}
+
+}  // namespace lesgo

@@ -322,6 +322,8 @@ class SolverBase {
   virtual void profile(int enable) = 0;
   virtual std::string profile_report() = 0;
   virtual void* stream() const = 0;
+  virtual int tridag(const double* a, const double* b, const double* c, const double* r, double* u, int lh, int ny,
+                     int n) = 0;
 };
 
 template <typename R>
@@ -371,6 +373,7 @@ class Solver : public SolverBase {
   }
 
   ~Solver() override {
+    if (tri_gam_) cudaFree(tri_gam_);
     for (auto& r : prof_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
     for (void* p : allocs_) cudaFree(p);
@@ -671,6 +674,29 @@ class Solver : public SolverBase {
     return out + "}";
   }
   void* stream() const override { return (void*)st_; }
+
+  // Stand-alone tridag_array on caller device arrays; the gam scratch is
+  // owned by the handle and grows on demand.
+  int tridag(const double* a, const double* b, const double* c, const double* r, double* u, int lh, int ny,
+             int n) override {
+    const long long need = (long long)lh * ny * n;
+    if (need > tri_gam_n_) {
+      if (tri_gam_) cudaFree(tri_gam_);
+      tri_gam_ = nullptr;
+      CK(cudaMalloc(&tri_gam_, need * sizeof(double)));
+      tri_gam_n_ = need;
+    }
+    CK(cudaMemsetAsync(err_, 0, sizeof(int), st_));
+    const int ncol = (lh - 1) * ny;
+    pre();
+    k_tridag<<<(ncol + 127) / 128, 128, 0, st_>>>(a, b, c, (const double2*)r, (double2*)u, tri_gam_, lh, ny, n, err_);
+    post("tridag_array", (double)need * (3 * 8 + 2 * 16));
+    int e = 0;
+    CK(cudaMemcpyAsync(&e, err_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    if (e) { CK(cudaMemset(err_, 0, sizeof(int))); return LESGO_ERR_NUMERIC; }
+    return LESGO_OK;
+  }
 
   int launches_per_step(int with_sgs) const override {
     for (auto& kv : launch_count_) {
@@ -1151,6 +1177,8 @@ class Solver : public SolverBase {
   TurbineHost th_;
   TurbDev td_{};
   long long* cols_ = nullptr;
+  double* tri_gam_ = nullptr;
+  long long tri_gam_n_ = 0;
   int jt_ = 0, jt_total_ = 0;
   bool F_LM_MM_init_ = false, F_QN_NN_init_ = false;
   bool use_graphs_ = true, graphs_allowed_ = true;
@@ -1376,3 +1404,14 @@ int lesgo_gpu_get_stream(const lesgo_handle_t* h, void** stream) {
   return LESGO_OK;
 }
 }  // extern "C"
+
+extern "C" int lesgo_gpu_tridag_array(lesgo_handle_t* h, const double* a, const double* b, const double* c,
+                                      const double* r, double* u, int lh, int ny, int n) {
+  if (!a || !b || !c || !r || !u || lh < 2 || ny < 1 || n < 1) return LESGO_ERR_ARG;
+  int rc = LESGO_OK;
+  int g = guarded(h, [&] { rc = h->s->tridag(a, b, c, r, u, lh, ny, n); });
+  if (g != LESGO_OK) return g;
+  if (rc != LESGO_OK) h->err = "tridag_array: zero pivot";
+  return rc;
+}
+

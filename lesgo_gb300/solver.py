@@ -183,6 +183,12 @@ class LesgoGPU:
     def project(self):
         self._check(self._lib.lesgo_gpu_project(self._h))
 
+    def tridag_array(self, a_ptr: int, b_ptr: int, c_ptr: int, r_ptr: int, u_ptr: int, lh: int, ny: int, n: int):
+        """tridag_array.f90:166-246 on device arrays (addresses of FP64
+        buffers in the reference layout)."""
+        self._check(self._lib.lesgo_gpu_tridag_array(self._h, C.c_void_p(a_ptr), C.c_void_p(b_ptr), C.c_void_p(c_ptr),
+                                                     C.c_void_p(r_ptr), C.c_void_p(u_ptr), lh, ny, n))
+
     def step_reference_order(self):
         """One time step through the stand-alone entry points in the order
         of main.f90:130-344 (the drop-in call sequence)."""
