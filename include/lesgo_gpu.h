@@ -174,6 +174,18 @@ int lesgo_gpu_project(lesgo_handle_t* h);
  * returns when done; LESGO_ERR_NUMERIC on a zero pivot. */
 int lesgo_gpu_tridag_array(lesgo_handle_t* h, const double* a, const double* b, const double* c,
                            const double* r, double* u, int lh, int ny, int n);
+/* Allocation-free variant of lesgo_gpu_tridag_array.  No counterpart in
+ * the reference.  For callers that cannot allocate device memory (they own
+ * every buffer through their own pool, must not stall on cudaMalloc, or
+ * hold no handle): it needs no handle and allocates nothing.  Scratch is a
+ * fixed 16 MiB array inside the library (lh*ny*n <= 2^21 doubles; larger
+ * problems get LESGO_ERR_ARG), held on every GPU that loads the library.
+ * The first call on a device looks up that array's address (make it
+ * outside stream capture).  Calls share the array: calls whose GPU work
+ * overlaps race.  Launches on `stream` (NULL: default stream) and returns
+ * when done; errors are described by lesgo_gpu_last_error(NULL). */
+int lesgo_gpu_tridag_array_noalloc(const double* a, const double* b, const double* c, const double* r,
+                                   double* u, int lh, int ny, int n, void* stream);
 
 /* ---- fused time loop ---------------------------------------------------- */
 /* Advance nsteps full time steps (main.f90:130-344) with fused kernels and

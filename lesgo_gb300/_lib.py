@@ -87,6 +87,8 @@ SIGNATURES = {
     "lesgo_gpu_rhs_sub_dp": (_I, [_H]),
     "lesgo_gpu_project": (_I, [_H]),
     "lesgo_gpu_tridag_array": (_I, [_H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _I, _I, _I]),
+    "lesgo_gpu_tridag_array_noalloc": (_I, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _I, _I, _I,
+                                            C.c_void_p]),
     "lesgo_gpu_step": (_I, [_H, _I]),
     "lesgo_gpu_sync": (_I, [_H]),
     "lesgo_gpu_diag": (_I, [_H, _D, _D, _D, _D]),

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -1415,3 +1416,83 @@ extern "C" int lesgo_gpu_tridag_array(lesgo_handle_t* h, const double* a, const 
   return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free tridiagonal solve.
+//
+// lesgo_gpu_tridag_array_noalloc runs the same Thomas kernel as
+// lesgo_gpu_tridag_array but takes its scratch from a fixed array compiled
+// into this library instead of asking the CUDA allocator.  It serves
+// callers that must not allocate device memory themselves: code that owns
+// every device buffer through its own pool or framework, loops that must not
+// stall on cudaMalloc/cudaFree (which can synchronise the device), and
+// callers that hold no solver handle at all.
+//
+// The scratch array is a file-scope __device__ array of kTridagScratchDoubles
+// doubles (16 MiB); every GPU that loads the library holds it until the
+// process exits.  Host code may not use the array's name as a device
+// address, so the first call on each device looks the address up with
+// cudaGetSymbolAddress while that device is current and caches it; make that
+// first call outside any stream capture.  All calls on a device share the
+// array and it keeps the previous call's contents (the solve writes every
+// scratch entry before reading it; the error flag is cleared each call), so
+// calls whose GPU work overlaps in time race on it: issue them in order, on
+// one stream or with events between them.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr long long kTridagScratchDoubles = 1LL << 21;
+__device__ __align__(256) double g_tridag_scratch[kTridagScratchDoubles];
+__device__ __align__(256) int g_tridag_err;
+
+struct NoAllocSlot { double* scratch = nullptr; int* err = nullptr; };
+std::mutex g_noalloc_mu;
+std::map<int, NoAllocSlot> g_noalloc_slots;
+
+int noalloc_fail(int code, const std::string& msg) {
+  g_create_err = msg;
+  return code;
+}
+}  // namespace
+
+extern "C" int lesgo_gpu_tridag_array_noalloc(const double* a, const double* b, const double* c, const double* r,
+                                              double* u, int lh, int ny, int n, void* stream) {
+  if (!a || !b || !c || !r || !u || lh < 2 || ny < 1 || n < 1)
+    return noalloc_fail(LESGO_ERR_ARG, "tridag_array_noalloc: null pointer or bad size");
+  const long long need = (long long)lh * ny * n;
+  if (need > kTridagScratchDoubles)
+    return noalloc_fail(LESGO_ERR_ARG, "tridag_array_noalloc: lh*ny*n = " + std::to_string(need) +
+                                           " exceeds the fixed scratch of " + std::to_string(kTridagScratchDoubles) +
+                                           " doubles");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return noalloc_fail(LESGO_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  NoAllocSlot slot;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    auto it = g_noalloc_slots.find(dev);
+    if (it == g_noalloc_slots.end()) {
+      NoAllocSlot s;
+      e = cudaGetSymbolAddress((void**)&s.scratch, g_tridag_scratch);
+      if (e != cudaSuccess)
+        return noalloc_fail(LESGO_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+      e = cudaGetSymbolAddress((void**)&s.err, g_tridag_err);
+      if (e != cudaSuccess)
+        return noalloc_fail(LESGO_ERR_CUDA, std::string("cudaGetSymbolAddress(flag): ") + cudaGetErrorString(e));
+      it = g_noalloc_slots.emplace(dev, s).first;
+    }
+    slot = it->second;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  e = cudaMemsetAsync(slot.err, 0, sizeof(int), st);
+  if (e != cudaSuccess) return noalloc_fail(LESGO_ERR_CUDA, std::string("clear flag: ") + cudaGetErrorString(e));
+  const int ncol = (lh - 1) * ny;
+  lesgo::k_tridag<<<(ncol + 127) / 128, 128, 0, st>>>(a, b, c, (const double2*)r, (double2*)u, slot.scratch, lh, ny, n,
+                                                        slot.err);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return noalloc_fail(LESGO_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  int flag = 0;
+  e = cudaMemcpyAsync(&flag, slot.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return noalloc_fail(LESGO_ERR_CUDA, std::string("tridag_array_noalloc: ") + cudaGetErrorString(e));
+  if (flag) return noalloc_fail(LESGO_ERR_NUMERIC, "tridag_array_noalloc: zero pivot");
+  return LESGO_OK;
+}
