@@ -212,6 +212,29 @@ int lesgo_gpu_turbine_state(lesgo_handle_t* h, double* u_d_T, double* f_n, doubl
  * given kind (0: normal step, 1: step with the dynamic SGS update). */
 int lesgo_gpu_launches_per_step(const lesgo_handle_t* h, int with_sgs_update);
 
+/* ---- batches (no reference counterpart: the reference runs one instance
+ * per MPI job) ------------------------------------------------------------
+ * A batch handle holds `capacity` slots of one grid size; every kernel of a
+ * step processes all active instances in one launch.  Instances have their
+ * own roughness length, IC seed, actuator disks and step counters; they
+ * share the other parameters of `p` (whose zo / turbines are ignored here).
+ * The stage entry points and lesgo_gpu_step act on every active instance;
+ * per-instance access goes through the *_inst calls with the id from
+ * lesgo_gpu_batch_add.  Removing an instance moves the last one into its
+ * slot (ids stay valid). */
+int lesgo_gpu_batch_create(const lesgo_params_t* p, int capacity, lesgo_handle_t** h);
+int lesgo_gpu_batch_add(lesgo_handle_t* h, double zo, uint64_t seed, int n_turbines,
+                        const lesgo_turbine_t* turbines, int* id);
+int lesgo_gpu_batch_remove(lesgo_handle_t* h, int id);
+int lesgo_gpu_batch_size(const lesgo_handle_t* h, int* active, int* capacity);
+int lesgo_gpu_set_field_inst(lesgo_handle_t* h, int id, int field, const double* host, int lbz, int nzhi);
+int lesgo_gpu_get_field_inst(lesgo_handle_t* h, int id, int field, double* host, int lbz, int nzhi);
+int lesgo_gpu_diag_inst(lesgo_handle_t* h, int id, double* rmsdiv, double* ke, double* cfl, double* tau_bot);
+int lesgo_gpu_counters_inst(lesgo_handle_t* h, int id, int* jt, int* jt_total);
+int lesgo_gpu_turbine_state_inst(lesgo_handle_t* h, int id, double* u_d_T, double* f_n, double* power, int n);
+/* Device bytes a handle of this grid and capacity allocates (admission). */
+int lesgo_gpu_footprint(const lesgo_params_t* p, int capacity, long long* bytes);
+
 /* ---- instrumentation (no reference counterpart; the reference only
  * prints wall-clock times, main.f90:359-436) --------------------------- */
 /* enable != 0: run steps eagerly (no graph replay) with a CUDA event pair

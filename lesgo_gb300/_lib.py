@@ -95,6 +95,16 @@ SIGNATURES = {
     "lesgo_gpu_counters": (_I, [_H, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_turbine_state": (_I, [_H, _D, _D, _D, _I]),
     "lesgo_gpu_launches_per_step": (_I, [_H, _I]),
+    "lesgo_gpu_batch_create": (_I, [C.POINTER(Params), _I, C.POINTER(_H)]),
+    "lesgo_gpu_batch_add": (_I, [_H, C.c_double, C.c_uint64, _I, C.POINTER(Turbine), C.POINTER(_I)]),
+    "lesgo_gpu_batch_remove": (_I, [_H, _I]),
+    "lesgo_gpu_batch_size": (_I, [_H, C.POINTER(_I), C.POINTER(_I)]),
+    "lesgo_gpu_set_field_inst": (_I, [_H, _I, _I, C.c_void_p, _I, _I]),
+    "lesgo_gpu_get_field_inst": (_I, [_H, _I, _I, C.c_void_p, _I, _I]),
+    "lesgo_gpu_diag_inst": (_I, [_H, _I, _D, _D, _D, _D]),
+    "lesgo_gpu_counters_inst": (_I, [_H, _I, C.POINTER(_I), C.POINTER(_I)]),
+    "lesgo_gpu_turbine_state_inst": (_I, [_H, _I, _D, _D, _D, _I]),
+    "lesgo_gpu_footprint": (_I, [C.POINTER(Params), _I, C.POINTER(C.c_longlong)]),
     "lesgo_gpu_profile": (_I, [_H, _I]),
     "lesgo_gpu_profile_report": (_I, [_H, C.c_char_p, _I]),
     "lesgo_gpu_get_stream": (_I, [_H, C.POINTER(C.c_void_p)]),

@@ -12,7 +12,7 @@ namespace lesgo {
 // ---------------------------------------------------------------------------
 struct WallOut { double txz, tyz, dudz, dvdz; };
 
-__device__ __forceinline__ WallOut wall_bottom(const KP& kp, double u1f, double v1f, double u1, double v1) {
+__device__ __forceinline__ WallOut wall_bottom(const KP& kp, double zo, double u1f, double v1f, double u1, double v1) {
   WallOut o{0.0, 0.0, 0.0, 0.0};
   if (kp.lbc == 1) {                      // ws_dns_lbc (:131-148)
     o.dudz = (u1 - kp.ubot) / (0.5 * kp.dz);
@@ -20,7 +20,7 @@ __device__ __forceinline__ WallOut wall_bottom(const KP& kp, double u1f, double 
     o.txz = -kp.nu_nd * o.dudz;
     o.tyz = -kp.nu_nd * o.dvdz;
   } else if (kp.lbc == 2) {               // ws_equilibrium_lbc (:171-219)
-    const double denom = log(0.5 * kp.dz / kp.zo);
+    const double denom = log(0.5 * kp.dz / zo);
     const double u_avg = sqrt(u1f * u1f + v1f * v1f);
     const double ustar = u_avg * kp.vonk / denom;
     const double c = -(ustar * ustar) / u_avg;
@@ -32,7 +32,7 @@ __device__ __forceinline__ WallOut wall_bottom(const KP& kp, double u1f, double 
   return o;
 }
 
-__device__ __forceinline__ WallOut wall_top(const KP& kp, double utf, double vtf, double ut, double vt) {
+__device__ __forceinline__ WallOut wall_top(const KP& kp, double zo, double utf, double vtf, double ut, double vt) {
   WallOut o{0.0, 0.0, 0.0, 0.0};
   if (kp.ubc == 1) {                      // ws_dns_ubc (:151-168)
     o.dudz = (kp.utop - ut) / (0.5 * kp.dz);
@@ -40,7 +40,7 @@ __device__ __forceinline__ WallOut wall_top(const KP& kp, double utf, double vtf
     o.txz = -kp.nu_nd * o.dudz;
     o.tyz = -kp.nu_nd * o.dvdz;
   } else if (kp.ubc == 2) {               // ws_equilibrium_ubc (:222-255)
-    const double denom = log(0.5 * kp.dz / kp.zo);
+    const double denom = log(0.5 * kp.dz / zo);
     const double u_avg = sqrt(utf * utf + vtf * vtf);
     const double ustar = u_avg * kp.vonk / denom;
     const double c = (ustar * ustar) / u_avg;
@@ -74,7 +74,6 @@ struct ColArgs {
   KP kp;
   double delta2;
   int chunk;
-  int cs_fill;                          // Cs_opt2 = 0.03 this step (sgs_stag_util.f90:187-189)
 };
 
 template <typename R>
@@ -90,8 +89,12 @@ __global__ void __launch_bounds__(256) k_column(ColArgs<R> a) {
   const int k0 = 1 + blockIdx.y * a.chunk;
   if (k0 > nz) return;
   const int k1 = min(nz + 1, k0 + a.chunk);
+  const int inst = blockIdx.z;
   const long long P = kp.plane;
-  const long long c0 = (long long)j * kp.ld + i;
+  const long long cw = inst * P + (long long)j * kp.ld + i;          // wall planes (ld, ny) per instance
+  const long long c0 = inst * kp.istride + (long long)j * kp.ld + i;  // 3-D fields
+  const double zo = kp.zo_i[inst];
+  const bool cs_fill = (kp.iflags[inst] & IF_CSFILL) != 0;
   const R inv_dz = (R)(1.0 / kp.dz);
   const R h = (R)0.5;
 
@@ -100,13 +103,13 @@ __global__ void __launch_bounds__(256) k_column(ColArgs<R> a) {
   if (FLAGS & COL_DDZ) {
     if (k0 == 1) {
       double uf = 0, vf = 0;
-      if (kp.lbc == 2) { uf = a.wb_u[c0]; vf = a.wb_v[c0]; }
-      wb = wall_bottom(kp, uf, vf, (double)a.u[P + c0], (double)a.v[P + c0]);
+      if (kp.lbc == 2) { uf = a.wb_u[cw]; vf = a.wb_v[cw]; }
+      wb = wall_bottom(kp, zo, uf, vf, (double)a.u[P + c0], (double)a.v[P + c0]);
     }
     if (k1 >= nz) {
       double uf = 0, vf = 0;
-      if (kp.ubc == 2) { uf = a.wt_u[c0]; vf = a.wt_v[c0]; }
-      wt = wall_top(kp, uf, vf, (double)a.u[(nz - 1) * P + c0], (double)a.v[(nz - 1) * P + c0]);
+      if (kp.ubc == 2) { uf = a.wt_u[cw]; vf = a.wt_v[cw]; }
+      wt = wall_top(kp, zo, uf, vf, (double)a.u[(nz - 1) * P + c0], (double)a.v[(nz - 1) * P + c0]);
     }
   }
   auto uz_at = [&](int k) -> R {
@@ -185,7 +188,7 @@ __global__ void __launch_bounds__(256) k_column(ColArgs<R> a) {
     }
     if (FLAGS & COL_TAU) {
       R cs;
-      if (a.cs_fill) {
+      if (cs_fill) {
         cs = (R)0.03;
         if (k < k1) a.Cs[q] = cs;
       } else {
@@ -231,17 +234,29 @@ __global__ void __launch_bounds__(256) k_column(ColArgs<R> a) {
   }
 }
 
+// Flat thread index over (instance, level 1..nz, j, i < nx) -> field offset.
+struct PtIdx { int inst, k, j, i; long long q; };
+__device__ __forceinline__ PtIdx pt_index(long long t, const KP& kp) {
+  PtIdx r;
+  r.i = (int)(t % kp.nx);
+  long long rr = t / kp.nx;
+  r.j = (int)(rr % kp.ny);
+  rr /= kp.ny;
+  r.k = 1 + (int)(rr % kp.nz);
+  r.inst = (int)(rr / kp.nz);
+  r.q = r.inst * kp.istride + (long long)r.k * kp.plane + (long long)r.j * kp.ld + r.i;
+  return r;
+}
+
 // Plain staggered z-derivatives for the stand-alone entry points.
 // uv: dfdz(k) = (f(k)-f(k-1))/dz, k = 2..nz; w: dfdz(k) = (f(k+1)-f(k))/dz, k = 1..nz-1.
 template <typename R, bool UV>
 __global__ void k_ddz(const R* __restrict__ f, R* __restrict__ dfdz, KP kp) {
-  const long long n = (long long)kp.nx * kp.ny * kp.nz;
+  const long long n = (long long)kp.nx * kp.ny * kp.nz * kp.ninst;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = t % kp.nx;
-    const long long r = t / kp.nx;
-    const int j = r % kp.ny;
-    const int k = 1 + (int)(r / kp.ny);
-    const long long q = k * kp.plane + (long long)j * kp.ld + i;
+    const PtIdx x = pt_index(t, kp);
+    const int k = x.k;
+    const long long q = x.q;
     const R c = (R)(1.0 / kp.dz);
     if (UV) { if (k >= 2) dfdz[q] = c * (f[q] - f[q - kp.plane]); }
     else    { if (k <= kp.nz - 1) dfdz[q] = c * (f[q + kp.plane] - f[q]); }
@@ -255,12 +270,15 @@ __global__ void k_wall(const R* u, const R* v, const R* wb_u, const R* wb_v, con
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= kp.nx * kp.ny) return;
   const int j = col / kp.nx, i = col - j * kp.nx;
-  const long long c0 = (long long)j * kp.ld + i;
+  const int inst = blockIdx.y;
   const long long P = kp.plane;
+  const long long cw = inst * P + (long long)j * kp.ld + i;
+  const long long c0 = inst * kp.istride + (long long)j * kp.ld + i;
   const int nz = kp.nz;
-  WallOut b = wall_bottom(kp, kp.lbc == 2 ? (double)wb_u[c0] : 0.0, kp.lbc == 2 ? (double)wb_v[c0] : 0.0,
+  const double zo = kp.zo_i[inst];
+  WallOut b = wall_bottom(kp, zo, kp.lbc == 2 ? (double)wb_u[cw] : 0.0, kp.lbc == 2 ? (double)wb_v[cw] : 0.0,
                           (double)u[P + c0], (double)v[P + c0]);
-  WallOut t = wall_top(kp, kp.ubc == 2 ? (double)wt_u[c0] : 0.0, kp.ubc == 2 ? (double)wt_v[c0] : 0.0,
+  WallOut t = wall_top(kp, zo, kp.ubc == 2 ? (double)wt_u[cw] : 0.0, kp.ubc == 2 ? (double)wt_v[cw] : 0.0,
                        (double)u[(nz - 1) * P + c0], (double)v[(nz - 1) * P + c0]);
   txz[P + c0] = (R)b.txz; tyz[P + c0] = (R)b.tyz; dudz[P + c0] = (R)b.dudz; dvdz[P + c0] = (R)b.dvdz;
   const long long qt = nz * P + c0;
@@ -285,15 +303,14 @@ __device__ __forceinline__ double fmodulo(double a, double p) { return a - floor
 template <typename R>
 __global__ void k_interp(InterpArgs<R> a) {
   const KP& kp = a.kp;
-  const long long n = (long long)kp.nx * kp.ny * kp.nz;
+  const long long n = (long long)kp.nx * kp.ny * kp.nz * kp.ninst;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  const int i = t % kp.nx;
-  const long long r = t / kp.nx;
-  const int j = r % kp.ny;
-  const int k = 1 + (int)(r / kp.ny);
+  const PtIdx x_ = pt_index(t, kp);
+  const int i = x_.i, j = x_.j, k = x_.k;
   const long long P = kp.plane;
-  const long long q = k * P + (long long)j * kp.ld + i;
+  const long long q = x_.q;
+  const long long ib = x_.inst * kp.istride;
   const int nz = kp.nz;
   const double ldt = kp.lagran_dt, dz = kp.dz;
   const double x = i * kp.dx, y = j * kp.dy;
@@ -341,7 +358,7 @@ __global__ void k_interp(InterpArgs<R> a) {
     kst1 = kst + 1;
     zdiff = zq - zwc(kst);
   }
-  const long long b00 = (long long)(jst - 1) * kp.ld, b01 = (long long)(jst1 - 1) * kp.ld;
+  const long long b00 = ib + (long long)(jst - 1) * kp.ld, b01 = ib + (long long)(jst1 - 1) * kp.ld;
   const int i0 = ist - 1, i1 = ist1 - 1;
   const long long z0 = kst * P, z1 = kst1 * P;
 #pragma unroll
@@ -373,31 +390,41 @@ struct ThomasArgs {
   double* gam;                   // index m*P, m = 0..nz+1
   const double *kxw, *kyw;
   double dz;
-  int nz, ny, K;
+  int nz, ny, K, ninst;
   int* err;
 };
 
 __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long P = (long long)a.ny * a.K;
-  if (t >= P) return;
+  if (gt >= P * a.ninst) return;
+  const int inst = (int)(gt / P);
+  const int t = (int)(gt - inst * P);
   const int jy = t / a.K, kx = t - jy * a.K;
   const int nz = a.nz, n = nz + 1;
   const double dz = a.dz;
+  // per-instance views: H* [inst][nz][P], Hb/Ht [inst][2][P], phat [inst][nz+1][P], gam [inst][nz+2][P]
+  const double2* Hx = a.Hx + (long long)inst * nz * P;
+  const double2* Hy = a.Hy + (long long)inst * nz * P;
+  const double2* Hz = a.Hz + (long long)inst * nz * P;
+  const double2* Hb = a.Hb + (long long)inst * 2 * P;
+  const double2* Ht = a.Ht + (long long)inst * 2 * P;
+  double2* phat = a.phat + (long long)inst * (nz + 1) * P;
+  double* gam = a.gam + (long long)inst * (nz + 2) * P;
   if (jy == a.ny / 2) {
-    for (int l = 0; l <= nz; ++l) a.phat[l * P + t] = make_double2(0.0, 0.0);
+    for (int l = 0; l <= nz; ++l) phat[l * P + t] = make_double2(0.0, 0.0);
     return;
   }
   if (kx == 0 && jy == 0) {
     double2 p = make_double2(0.0, 0.0);
-    a.phat[t] = p;
-    const double2 hb = a.Hb[t];
+    phat[t] = p;
+    const double2 hb = Hb[t];
     p = make_double2(p.x - dz * hb.x, p.y - dz * hb.y);
-    a.phat[P + t] = p;
+    phat[P + t] = p;
     for (int jz = 2; jz <= nz; ++jz) {
-      const double2 hz = a.Hz[(jz - 1) * P + t];
+      const double2 hz = Hz[(jz - 1) * P + t];
       p = make_double2(p.x + hz.x * dz, p.y + hz.y * dz);
-      a.phat[jz * P + t] = p;
+      phat[jz * P + t] = p;
     }
     return;
   }
@@ -406,40 +433,40 @@ __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
   const double kxv = a.kxw[kx], kyv = a.kyw[jy];
   const double bmid = -(kxv * kxv + kyv * kyv + 2.0 * c3);
   // m = 1: b = -1, c = 1, r = -dz * rbottomw
-  const double2 hb = a.Hb[t];
+  const double2 hb = Hb[t];
   double2 up = make_double2((-dz * hb.x) / -1.0, (-dz * hb.y) / -1.0);
-  a.phat[t] = up;
+  phat[t] = up;
   double bet = -1.0;
-  double2 hzp = a.Hz[t];   // level 1
+  double2 hzp = Hz[t];   // level 1
   for (int j = 2; j <= n; ++j) {
     double aj, bj, r_x, r_y;
     const double cprev = (j == 2) ? 1.0 : c3;
     if (j <= nz) {
       aj = c3; bj = bmid;
-      const double2 hx = a.Hx[(j - 2) * P + t], hy = a.Hy[(j - 2) * P + t];
-      const double2 hz = a.Hz[(j - 1) * P + t];
+      const double2 hx = Hx[(j - 2) * P + t], hy = Hy[(j - 2) * P + t];
+      const double2 hz = Hz[(j - 1) * P + t];
       // i kx Hx + i ky Hy + (Hz(j) - Hz(j-1)) / dz
       r_x = (-hx.y * kxv) + (-hy.y * kyv) + (hz.x - hzp.x) * c4;
       r_y = (hx.x * kxv) + (hy.x * kyv) + (hz.y - hzp.y) * c4;
       hzp = hz;
     } else {
       aj = -1.0; bj = 1.0;
-      const double2 ht = a.Ht[t];
+      const double2 ht = Ht[t];
       r_x = -dz * ht.x; r_y = -dz * ht.y;
     }
     const double g = cprev / bet;
     bet = bj - aj * g;
     if (bet == 0.0) { atomicExch(a.err, 1); bet = 1.0; }
     up = make_double2((r_x - aj * up.x) / bet, (r_y - aj * up.y) / bet);
-    a.gam[j * P + t] = g;
-    a.phat[(j - 1) * P + t] = up;
+    gam[j * P + t] = g;
+    phat[(j - 1) * P + t] = up;
   }
   double2 un = up;   // u(n)
   for (int j = n - 1; j >= 1; --j) {
-    const double g = a.gam[(j + 1) * P + t];
-    double2 uj = a.phat[(j - 1) * P + t];
+    const double g = gam[(j + 1) * P + t];
+    double2 uj = phat[(j - 1) * P + t];
     uj = make_double2(uj.x - g * un.x, uj.y - g * un.y);
-    a.phat[(j - 1) * P + t] = uj;
+    phat[(j - 1) * P + t] = uj;
     un = uj;
   }
 }
@@ -448,15 +475,13 @@ __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
 // (FUSED: RHSz -= dpdz, project w, boundary conditions) or just dpdz.
 template <typename R, bool FUSED>
 __global__ void k_wproj(const R* __restrict__ p, R* dpdz, R* RHSz, R* u, R* v, R* w, KP kp) {
-  const long long n = (long long)kp.nx * kp.ny * kp.nz;
+  const long long n = (long long)kp.nx * kp.ny * kp.nz * kp.ninst;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  const int i = t % kp.nx;
-  const long long r = t / kp.nx;
-  const int j = r % kp.ny;
-  const int k = 1 + (int)(r / kp.ny);
+  const PtIdx x = pt_index(t, kp);
+  const int k = x.k;
   const long long P = kp.plane;
-  const long long q = k * P + (long long)j * kp.ld + i;
+  const long long q = x.q;
   const R d = (p[q] - p[q - P]) / (R)kp.dz;
   if (!FUSED) { dpdz[q] = d; return; }
   RHSz[q] = RHSz[q] - d;
@@ -472,14 +497,12 @@ __global__ void k_wproj(const R* __restrict__ p, R* dpdz, R* RHSz, R* u, R* v, R
 // forcing.f90:149-244 stand-alone projection (two kernels: update, then BCs).
 template <typename R>
 __global__ void k_project(const R* dpdx, const R* dpdy, const R* dpdz, R* u, R* v, R* w, KP kp) {
-  const long long n = (long long)kp.nx * kp.ny * kp.nz;
+  const long long n = (long long)kp.nx * kp.ny * kp.nz * kp.ninst;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  const int i = t % kp.nx;
-  const long long r = t / kp.nx;
-  const int j = r % kp.ny;
-  const int k = 1 + (int)(r / kp.ny);
-  const long long q = k * kp.plane + (long long)j * kp.ld + i;
+  const PtIdx x = pt_index(t, kp);
+  const int k = x.k;
+  const long long q = x.q;
   const R dt = (R)kp.dt, t1 = (R)kp.tadv1;
   if (k <= kp.nz - 1) {
     u[q] = u[q] + dt * (-t1 * dpdx[q]);
@@ -491,8 +514,9 @@ __global__ void k_project(const R* dpdx, const R* dpdy, const R* dpdz, R* u, R* 
 template <typename R>
 __global__ void k_project_bc(R* u, R* v, R* w, KP kp) {
   const long long pl = kp.plane;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= pl) return;
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gt >= pl * kp.ninst) return;
+  const long long t = (gt / pl) * kp.istride + gt % pl;
   const int nz = kp.nz;
   if (kp.ubc == 0) { u[nz * pl + t] = u[(nz - 1) * pl + t]; v[nz * pl + t] = v[(nz - 1) * pl + t]; }
   w[nz * pl + t] = (R)0;
@@ -506,9 +530,10 @@ __global__ void k_rhs_assemble(R* RHSx, R* RHSy, R* RHSz, const R* divtx, const 
                                const R* fxa, const R* fya, const R* fza, KP kp) {
   const long long pl = kp.plane;
   const long long n = pl * kp.nz;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const long long q = pl + t;   // levels 1..nz
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gt >= n * kp.ninst) return;
+  const long long t = gt % n;
+  const long long q = (gt / n) * kp.istride + pl + t;   // levels 1..nz
   const int k = 1 + (int)(t / pl);
   if (k <= kp.nz - 1) {
     R x = -RHSx[q] - divtx[q], y = -RHSy[q] - divty[q], z = -RHSz[q] - divtz[q];
@@ -525,9 +550,10 @@ __global__ void k_ab2(R* u, R* v, R* w, const R* RHSx, const R* RHSy, const R* R
                       const R* fx, const R* fy, const R* fz, KP kp) {
   const long long pl = kp.plane;
   const long long n = pl * kp.nz;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const long long q = pl + t;
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gt >= n * kp.ninst) return;
+  const long long t = gt % n;
+  const long long q = (gt / n) * kp.istride + pl + t;
   const int k = 1 + (int)(t / pl);
   const R dt = (R)kp.dt, t1 = (R)kp.tadv1, t2 = (R)kp.tadv2;
   if (k <= kp.nz - 1) {
@@ -541,9 +567,10 @@ template <typename R>
 __global__ void k_rhs_sub_dp(R* RHSx, R* RHSy, R* RHSz, const R* dpdx, const R* dpdy, const R* dpdz, KP kp) {
   const long long pl = kp.plane;
   const long long n = pl * kp.nz;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const long long q = pl + t;
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gt >= n * kp.ninst) return;
+  const long long t = gt % n;
+  const long long q = (gt / n) * kp.istride + pl + t;
   const int k = 1 + (int)(t / pl);
   if (k <= kp.nz - 1) { RHSx[q] = RHSx[q] - dpdx[q]; RHSy[q] = RHSy[q] - dpdy[q]; }
   RHSz[q] = RHSz[q] - dpdz[q];
@@ -577,21 +604,23 @@ __device__ __forceinline__ double hash_pm1(uint64_t seed, uint64_t fld, uint64_t
   return 2.0 * u01 - 1.0;
 }
 
+// Writes instance `inst` (all levels) with its own seed and roughness.
 template <typename R>
-__global__ void k_ic(R* u, R* v, R* w, KP kp, uint64_t seed) {
+__global__ void k_ic(R* u, R* v, R* w, KP kp, uint64_t seed, int inst) {
   const long long pl = kp.plane;
   const long long n = pl * (kp.nz + 1);
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int k = (int)(t / pl);
-  const long long rr = t - (long long)k * pl;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t0 >= n) return;
+  const long long t = inst * kp.istride + t0;
+  const int k = (int)(t0 / pl);
+  const long long rr = t0 - (long long)k * pl;
   const int j = (int)(rr / kp.ld), i = (int)(rr - (long long)j * kp.ld);
   const int nz = kp.nz;
   double uu = 0, vv = 0, ww = 0;
   const int kk = (k == nz) ? nz - 1 : k;   // u(nz) = u(nz-1), v(nz) = v(nz-1)
   if (i < kp.nx && kk >= 1 && kk <= nz - 1) {
     const double zk = (kk - 0.5) * kp.dz;
-    const double ubar = (1.0 / 0.4) * log(zk / kp.zo);
+    const double ubar = (1.0 / 0.4) * log(zk / kp.zo_i[inst]);
     uu = ubar * (1.0 + 0.1 * hash_pm1(seed, 0, i, j, kk));
     vv = 0.1 * hash_pm1(seed, 1, i, j, kk);
     if (k >= 2 && k <= nz - 1) ww = 0.1 * hash_pm1(seed, 2, i, j, k);
@@ -605,7 +634,7 @@ __global__ void k_ic(R* u, R* v, R* w, KP kp, uint64_t seed) {
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(256) k_diag(const R* dudx, const R* dvdy, const R* dwdz, const R* u, const R* v,
-                                              const R* w, const R* txz, const R* tyz, KP kp, double* partial) {
+                                              const R* w, const R* txz, const R* tyz, KP kp, double* partial, int inst) {
   __shared__ double sh[7][256];
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   const long long n = (long long)kp.nx * kp.ny * (kp.nz - 1);
@@ -614,7 +643,7 @@ __global__ void __launch_bounds__(256) k_diag(const R* dudx, const R* dvdy, cons
     const long long r = t / kp.nx;
     const int j = r % kp.ny;
     const int k = 1 + (int)(r / kp.ny);
-    const long long q = k * kp.plane + (long long)j * kp.ld + i;
+    const long long q = inst * kp.istride + k * kp.plane + (long long)j * kp.ld + i;
     acc[0] += fabs((double)dudx[q] + (double)dvdy[q] + (double)dwdz[q]);
     const double tw = 0.5 * ((double)w[q] + (double)w[q + kp.plane]);
     acc[1] += (double)u[q] * u[q] + (double)v[q] * v[q] + tw * tw;
@@ -675,7 +704,8 @@ struct TurbDev {
 };
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_turb_disk(TurbDev td, const R* u, const R* v, const R* w, long long plane, int nz) {
+__global__ void __launch_bounds__(256) k_turb_disk(TurbDev td, const R* u, const R* v, const R* w, long long plane, int nz,
+                                                   long long istride) {
   __shared__ double sh[256];
   const int s = blockIdx.x;
   double acc = 0.0;
@@ -683,7 +713,7 @@ __global__ void __launch_bounds__(256) k_turb_disk(TurbDev td, const R* u, const
   for (int l = td.node_off[s] + threadIdx.x; l < td.node_off[s + 1]; l += blockDim.x) {
     const long long q = td.node_q[l];
     // interp_to_uv_grid (functions.f90:87-105): level nz repeats level nz-1
-    const long long qq = (q / plane >= nz) ? q - plane : q;
+    const long long qq = ((q % istride) / plane >= nz) ? q - plane : q;
     const double wuv = 0.5 * ((double)w[qq + plane] + (double)w[qq]);
     acc += td.dvol * td.node_ind[l] * (n0 * (double)u[q] + n1 * (double)v[q] + n2 * wuv);
   }

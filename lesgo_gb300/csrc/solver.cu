@@ -206,71 +206,78 @@ struct TurbineHost {
   std::vector<double> nhat, ctp, corr, dia;
 };
 
-static TurbineHost turbines_init_host(const Derived& d) {
+// Node lists of the actuator disks of every active instance, with absolute
+// offsets (instance base + level*plane + jy*ld + i).  Indicator tables are
+// cached by (thickness, diameter).
+using IndicatorCache = std::map<std::pair<double, double>, Indicator>;
+
+static TurbineHost turbines_build(const Derived& d, const std::vector<std::vector<lesgo_turbine_t>>& per_inst,
+                                  long long istride, IndicatorCache& cache) {
   TurbineHost th;
-  th.n = (int)d.turbines.size();
-  if (th.n == 0) return th;
   const auto& P = d.p;
-  std::vector<lesgo_turbine_t> ts = d.turbines;
   const double dx = d.dx, dy = d.dy, dz = d.dz;
-  for (auto& t : ts) t.thk = std::max(t.thk, dx * (double)1.01f);   // turbines.f90:180 (single-precision literal)
   const double diag = std::sqrt(dx * dx + dy * dy + dz * dz);
   const double delta1 = P.alpha1 * diag, delta2 = P.alpha2 * diag;
-  std::map<std::pair<double, double>, Indicator> cache;
   const long long plane = (long long)d.ld * d.ny;
   th.node_off.push_back(0);
-  for (int s = 0; s < th.n; ++s) {
-    const auto& t = ts[s];
-    auto key = std::make_pair(t.thk, t.dia);
-    if (!cache.count(key)) cache[key] = make_indicator(delta1, delta2, t.thk, t.dia);
-    const Indicator& ind = cache[key];
-    const double search_rad = 0.5 * t.dia + 3 * std::max(P.alpha1, P.alpha2) * diag;
-    const int imax = std::min((int)(search_rad / dx + 2), d.nx / 2);
-    const int jmax = std::min((int)(search_rad / dy + 2), d.ny / 2);
-    const double n1 = -std::cos(kPi * t.theta1 / 180.) * std::cos(kPi * t.theta2 / 180.);
-    const double n2 = -std::sin(kPi * t.theta1 / 180.) * std::cos(kPi * t.theta2 / 180.);
-    const double n3 = std::sin(kPi * t.theta2 / 180.);
-    const long long icp = nint_f(t.xloc / dx), jcp = nint_f(t.yloc / dy);
-    const double filt_max = ind.val(0.0, 0.0);
-    double sumA = 0.0;
-    std::vector<long long> q;
-    std::vector<double> fv;
-    for (int k = 1; k <= d.nz; ++k) {
-      if (k > d.nz_tot) continue;
-      const double zt = (k - 0.5) * dz;
-      for (long long j = jcp - jmax + 1; j <= jcp + jmax; ++j)
-        for (long long i = icp - imax + 1; i <= icp + imax; ++i) {
-          long long i2 = i, j2 = j;
-          double rx, ry;
-          if (i < 1) { i2 = ((i + d.nx - 1) % d.nx) + 1; rx = ((i2 - 1) * dx - P.L_x) - t.xloc; }
-          else if (i > d.nx) { i2 = ((i + d.nx - 1) % d.nx) + 1; rx = (P.L_x + (i2 - 1) * dx) - t.xloc; }
-          else rx = (i - 1) * dx - t.xloc;
-          if (j < 1) { j2 = ((j + d.ny - 1) % d.ny) + 1; ry = ((j2 - 1) * dy - P.L_y) - t.yloc; }
-          else if (j > d.ny) { j2 = ((j + d.ny - 1) % d.ny) + 1; ry = (P.L_y + (j2 - 1) * dy) - t.yloc; }
-          else ry = (j - 1) * dy - t.yloc;
-          const double rz = zt - t.height;
-          const double r = std::sqrt(rx * rx + ry * ry + rz * rz);
-          const double r_norm = std::fabs(rx * n1 + ry * n2 + rz * n3);
-          const double r_disk = std::sqrt(r * r - r_norm * r_norm);
-          const double filt = ind.val(r_disk, r_norm);
-          if (filt > P.filter_cutoff * filt_max) {
-            q.push_back((long long)k * plane + (j2 - 1) * d.ld + (i2 - 1));
-            fv.push_back(filt);
-            sumA += filt * dx * dy * dz;
+  std::vector<int> inst_of;
+  for (size_t inst = 0; inst < per_inst.size(); ++inst) {
+    const long long ib = (long long)inst * istride;
+    for (lesgo_turbine_t t : per_inst[inst]) {
+      t.thk = std::max(t.thk, dx * (double)1.01f);   // turbines.f90:180 (single-precision literal)
+      auto key = std::make_pair(t.thk, t.dia);
+      if (!cache.count(key)) cache[key] = make_indicator(delta1, delta2, t.thk, t.dia);
+      const Indicator& ind = cache[key];
+      const double search_rad = 0.5 * t.dia + 3 * std::max(P.alpha1, P.alpha2) * diag;
+      const int imax = std::min((int)(search_rad / dx + 2), d.nx / 2);
+      const int jmax = std::min((int)(search_rad / dy + 2), d.ny / 2);
+      const double n1 = -std::cos(kPi * t.theta1 / 180.) * std::cos(kPi * t.theta2 / 180.);
+      const double n2 = -std::sin(kPi * t.theta1 / 180.) * std::cos(kPi * t.theta2 / 180.);
+      const double n3 = std::sin(kPi * t.theta2 / 180.);
+      const long long icp = nint_f(t.xloc / dx), jcp = nint_f(t.yloc / dy);
+      const double filt_max = ind.val(0.0, 0.0);
+      double sumA = 0.0;
+      std::vector<long long> q;
+      std::vector<double> fv;
+      for (int k = 1; k <= d.nz; ++k) {
+        if (k > d.nz_tot) continue;
+        const double zt = (k - 0.5) * dz;
+        for (long long j = jcp - jmax + 1; j <= jcp + jmax; ++j)
+          for (long long i = icp - imax + 1; i <= icp + imax; ++i) {
+            long long i2 = i, j2 = j;
+            double rx, ry;
+            if (i < 1) { i2 = ((i + d.nx - 1) % d.nx) + 1; rx = ((i2 - 1) * dx - P.L_x) - t.xloc; }
+            else if (i > d.nx) { i2 = ((i + d.nx - 1) % d.nx) + 1; rx = (P.L_x + (i2 - 1) * dx) - t.xloc; }
+            else rx = (i - 1) * dx - t.xloc;
+            if (j < 1) { j2 = ((j + d.ny - 1) % d.ny) + 1; ry = ((j2 - 1) * dy - P.L_y) - t.yloc; }
+            else if (j > d.ny) { j2 = ((j + d.ny - 1) % d.ny) + 1; ry = (P.L_y + (j2 - 1) * dy) - t.yloc; }
+            else ry = (j - 1) * dy - t.yloc;
+            const double rz = zt - t.height;
+            const double r = std::sqrt(rx * rx + ry * ry + rz * rz);
+            const double r_norm = std::fabs(rx * n1 + ry * n2 + rz * n3);
+            const double r_disk = std::sqrt(r * r - r_norm * r_norm);
+            const double filt = ind.val(r_disk, r_norm);
+            if (filt > P.filter_cutoff * filt_max) {
+              q.push_back(ib + (long long)k * plane + (j2 - 1) * d.ld + (i2 - 1));
+              fv.push_back(filt);
+              sumA += filt * dx * dy * dz;
+            }
           }
-        }
+      }
+      for (size_t l = 0; l < q.size(); ++l) {
+        th.node_q.push_back(q[l]);
+        th.node_ind.push_back(fv[l] / sumA);
+      }
+      th.node_off.push_back((int)th.node_q.size());
+      th.nhat.insert(th.nhat.end(), {n1, n2, n3});
+      th.ctp.push_back(t.Ct_prime);
+      th.corr.push_back(P.adm_correction ? (1 + 0.25 * (1 - ind.M) * t.Ct_prime) : 1.0);
+      th.dia.push_back(t.dia);
+      inst_of.push_back((int)inst);
+      ++th.n;
     }
-    for (size_t l = 0; l < q.size(); ++l) {
-      th.node_q.push_back(q[l]);
-      th.node_ind.push_back(fv[l] / sumA);
-    }
-    th.node_off.push_back((int)th.node_q.size());
-    th.nhat.insert(th.nhat.end(), {n1, n2, n3});
-    th.ctp.push_back(t.Ct_prime);
-    th.corr.push_back(P.adm_correction ? (1 + 0.25 * (1 - ind.M) * t.Ct_prime) : 1.0);
-    th.dia.push_back(t.dia);
   }
-  // scatter list: the last turbine in order owns a shared node
+  // scatter list: within an instance the last turbine in order owns a shared node
   std::unordered_map<long long, std::pair<int, double>> owner;
   std::vector<long long> order;
   for (int s = 0; s < th.n; ++s)
@@ -283,22 +290,36 @@ static TurbineHost turbines_init_host(const Derived& d) {
     th.win_q.push_back(q);
     th.win_turb.push_back(owner[q].first);
     th.win_ind.push_back(owner[q].second);
-    const long long c = q % plane;
+    const long long inst = q / istride;
+    const long long c = inst * istride + (q % istride) % plane;
     if (!colset.count(c)) { colset[c] = 1; th.cols.push_back(c); }
   }
   return th;
 }
 
 // ---------------------------------------------------------------------------
-// Solver
+// Solver: `capacity` slots of one grid size, the first n_active of which hold
+// live LES instances (stable ids map to slots; removal compacts).  Every
+// kernel processes all active instances in one launch.  A single-instance
+// handle is a batch of capacity one.
 // ---------------------------------------------------------------------------
+struct InstanceSpec {
+  double zo;
+  uint64_t seed;
+  std::vector<lesgo_turbine_t> turbines;
+};
+
 class SolverBase {
  public:
   virtual ~SolverBase() {}
   virtual const Derived& der() const = 0;
-  virtual void set_field(int f, const double* h, int lbz, int nzhi) = 0;
-  virtual void get_field(int f, double* h, int lbz, int nzhi) = 0;
-  virtual void init_ic(uint64_t seed) = 0;
+  virtual int capacity() const = 0;
+  virtual int active() const = 0;
+  virtual int add_instance(const InstanceSpec& spec) = 0;
+  virtual void remove_instance(int id) = 0;
+  virtual void set_field(int id, int f, const double* h, int lbz, int nzhi) = 0;
+  virtual void get_field(int id, int f, double* h, int lbz, int nzhi) = 0;
+  virtual void init_ic(int id, uint64_t seed) = 0;
   virtual void filt_da(int f, int dx, int dy) = 0;
   virtual void ddxy(int f, int dx, int dy) = 0;   // dx or dy may be -1
   virtual void ddz(int f, int dfdz, bool uv) = 0;
@@ -316,9 +337,9 @@ class SolverBase {
   virtual void project() = 0;
   virtual void step(int n) = 0;
   virtual int sync() = 0;
-  virtual void diag(double* out4) = 0;
-  virtual void counters(int* jt, int* jt_total) const = 0;
-  virtual void turbine_state(double* udT, double* fn, double* pw, int n) = 0;
+  virtual void diag(int id, double* out4) = 0;
+  virtual void counters(int id, int* jt, int* jt_total) const = 0;
+  virtual void turbine_state(int id, double* udT, double* fn, double* pw, int n) = 0;
   virtual int launches_per_step(int with_sgs) const = 0;
   virtual void profile(int enable) = 0;
   virtual std::string profile_report() = 0;
@@ -327,12 +348,27 @@ class SolverBase {
                      int n) = 0;
 };
 
+// Device bytes of a handle (the admission footprint of a batch).
+static long long footprint_bytes(const Derived& d, int cap) {
+  const long long rs = d.p.precision == LESGO_FP64 ? 8 : 4;
+  const long long plane = (long long)d.ld * d.ny, pbig = (long long)d.ld_big * d.ny2;
+  const long long nf = (long long)(d.nz + 1) * plane;
+  const long long vs = (long long)d.nz * d.ny * d.K, vb = (long long)d.nz * d.ny2 * d.K, ps = (long long)d.ny * d.K;
+  long long b = 0;
+  b += (LESGO_NFIELDS + 4 + (d.turbines.empty() ? 0 : 1)) * nf * rs;   // fields, interpolation temps, fza on uv
+  b += 4 * plane * rs + 6 * (long long)(d.nz + 1) * pbig * rs;          // wall planes, 3/2-grid fields
+  b += (std::max({21 * vs, 6 * vs, 3 * vb}) + std::max({42 * vs, 6 * vb, 9 * vs}) + 4 * ps) * 2 * rs;   // spectra
+  b += (3 * vs + 2 * ps + (long long)(d.nz + 1) * ps) * 16 + (long long)(d.nz + 2) * ps * 8;           // FP64 pressure
+  return b * cap;
+}
+
 template <typename R>
 class Solver : public SolverBase {
   using T2 = cplx<R>;
 
  public:
-  explicit Solver(const Derived& d) : d_(d) {
+  Solver(const Derived& d, int capacity) : d_(d), cap_(capacity) {
+    if (capacity < 1) throw Error(LESGO_ERR_ARG, "capacity must be >= 1");
     CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
     const int nx = d_.nx, ny = d_.ny, nz = d_.nz;
     kp_.nx = nx; kp_.ny = ny; kp_.nz = nz; kp_.ld = d_.ld; kp_.lh = d_.lh;
@@ -347,29 +383,34 @@ class Solver : public SolverBase {
     kp_.nu_nd = d_.p.nu_molec / (d_.p.z_i * d_.p.u_star);
     kp_.ubot = d_.p.ubot; kp_.utop = d_.p.utop;
     kp_.lbc = d_.p.lbc_mom; kp_.ubc = d_.p.ubc_mom; kp_.use_mpf = d_.p.use_mean_p_force;
-    kp_.turbines = d_.turbines.empty() ? 0 : 1;
-    nfield_ = (long long)(nz + 1) * kp_.plane;
+    kp_.turbines = 0;
+    kp_.ninst = 0;
+    kp_.istride = (long long)(nz + 1) * kp_.plane;
+    kp_.istride_big = (long long)(nz + 1) * kp_.plane_big;
+    nfield_ = kp_.istride * cap_;
     for (int f = 0; f < LESGO_NFIELDS; ++f) F_[f] = alloc<R>(nfield_);
     for (int f = 0; f < 4; ++f) Ftmp_[f] = alloc<R>(nfield_);
-    for (int f = 0; f < 4; ++f) wall_[f] = alloc<R>(kp_.plane);
-    fza_uv_ = kp_.turbines ? alloc<R>(nfield_) : nullptr;
-    for (int f = 0; f < 6; ++f) big_[f] = alloc<R>((long long)(nz + 1) * kp_.plane_big);
-    vol_s_ = (long long)nz * ny * d_.K;
-    vol_b_ = (long long)nz * d_.ny2 * d_.K;
-    specA_ = alloc<T2>(std::max({21 * vol_s_, 6 * vol_s_, 3 * vol_b_}));
-    specB_ = alloc<T2>(std::max({42 * vol_s_, 6 * vol_b_, 9 * vol_s_}));
-    specC_ = alloc<T2>(4LL * ny * d_.K);
+    for (int f = 0; f < 4; ++f) wall_[f] = alloc<R>(kp_.plane * cap_);
+    for (int f = 0; f < 6; ++f) big_[f] = alloc<R>(kp_.istride_big * cap_);
+    vol1_s_ = (long long)nz * ny * d_.K;
+    vol1_b_ = (long long)nz * d_.ny2 * d_.K;
     const long long pl_s = (long long)ny * d_.K;
-    hspec_ = alloc<double2>(3 * vol_s_);
-    hplane_ = alloc<double2>(2 * pl_s);
-    phat_ = alloc<double2>((nz + 1) * pl_s);
-    gam_ = alloc<double>((nz + 2) * pl_s);
+    specA_ = alloc<T2>(std::max({21 * vol1_s_, 6 * vol1_s_, 3 * vol1_b_}) * cap_);
+    specB_ = alloc<T2>(std::max({42 * vol1_s_, 6 * vol1_b_, 9 * vol1_s_}) * cap_);
+    specC_ = alloc<T2>(4LL * pl_s * cap_);
+    hspec_ = alloc<double2>(3 * vol1_s_ * cap_);
+    hplane_ = alloc<double2>(2 * pl_s * cap_);
+    phat_ = alloc<double2>((nz + 1) * pl_s * cap_);
+    gam_ = alloc<double>((nz + 2) * pl_s * cap_);
     err_ = alloc<int>(1);
+    zo_d_ = alloc<double>(cap_);
+    flags_d_ = alloc<int>(cap_);
+    kp_.zo_i = zo_d_;
+    kp_.iflags = flags_d_;
     // LESGO_GRAPHS=0 replays nothing: every step launches eagerly
     if (const char* g = std::getenv("LESGO_GRAPHS")) graphs_allowed_ = std::strcmp(g, "0") != 0;
     use_graphs_ = graphs_allowed_;
     build_tables();
-    if (kp_.turbines) build_turbines();
     CK(cudaStreamSynchronize(st_));
   }
 
@@ -382,16 +423,55 @@ class Solver : public SolverBase {
   }
 
   const Derived& der() const override { return d_; }
+  int capacity() const override { return cap_; }
+  int active() const override { return (int)slots_.size(); }
+
+  // ---------------- instances --------------------------------------------------
+  int add_instance(const InstanceSpec& spec) override {
+    if ((int)slots_.size() >= cap_) throw Error(LESGO_ERR_NOMEM, "no free slot in this batch");
+    if (!(spec.zo > 0)) throw Error(LESGO_ERR_ARG, "zo must be positive");
+    Slot sl;
+    sl.id = next_id_++;
+    sl.spec = spec;
+    const int slot = (int)slots_.size();
+    slots_.push_back(sl);
+    sync_instance_params();
+    if (!spec.turbines.empty() || kp_.turbines) rebuild_turbines(-1, -1);
+    // fresh state: zero every field of the slot, then the seeded IC
+    for (int f = 0; f < LESGO_NFIELDS; ++f)
+      CK(cudaMemsetAsync(F_[f] + slot * kp_.istride, 0, kp_.istride * sizeof(R), st_));
+    ic_slot(slot, spec.seed);
+    CK(cudaStreamSynchronize(st_));
+    return sl.id;
+  }
+
+  void remove_instance(int id) override {
+    const int slot = slot_of(id);
+    const int last = (int)slots_.size() - 1;
+    if (slot != last) {
+      // move the last instance into the freed slot (fields and its state)
+      for (int f = 0; f < LESGO_NFIELDS; ++f)
+        CK(cudaMemcpyAsync(F_[f] + slot * kp_.istride, F_[f] + last * kp_.istride, kp_.istride * sizeof(R),
+                           cudaMemcpyDeviceToDevice, st_));
+      slots_[slot] = slots_[last];
+    }
+    const bool had_turbines = kp_.turbines != 0;
+    slots_.pop_back();
+    sync_instance_params();
+    if (had_turbines) rebuild_turbines(slot, last);
+    CK(cudaStreamSynchronize(st_));
+  }
 
   // ---------------- field access -----------------------------------------
   void check_range(int f, int lbz, int nzhi) const {
     if (f < 0 || f >= LESGO_NFIELDS) throw Error(LESGO_ERR_ARG, "bad field id");
     if (lbz < 0 || nzhi > d_.nz || nzhi < lbz) throw Error(LESGO_ERR_ARG, "levels outside 0..nz");
   }
-  void set_field(int f, const double* h, int lbz, int nzhi) override {
+  void set_field(int id, int f, const double* h, int lbz, int nzhi) override {
     check_range(f, lbz, nzhi);
+    const int slot = slot_of(id);
     const long long n = (long long)(nzhi - lbz + 1) * kp_.plane;
-    R* dst = F_[f] + (long long)lbz * kp_.plane;
+    R* dst = F_[f] + slot * kp_.istride + (long long)lbz * kp_.plane;
     if (std::is_same<R, double>::value) {
       CK(cudaMemcpyAsync(dst, h, n * sizeof(double), cudaMemcpyHostToDevice, st_));
     } else {
@@ -402,10 +482,11 @@ class Solver : public SolverBase {
     }
     CK(cudaStreamSynchronize(st_));
   }
-  void get_field(int f, double* h, int lbz, int nzhi) override {
+  void get_field(int id, int f, double* h, int lbz, int nzhi) override {
     check_range(f, lbz, nzhi);
+    const int slot = slot_of(id);
     const long long n = (long long)(nzhi - lbz + 1) * kp_.plane;
-    const R* src = F_[f] + (long long)lbz * kp_.plane;
+    const R* src = F_[f] + slot * kp_.istride + (long long)lbz * kp_.plane;
     if (std::is_same<R, double>::value) {
       CK(cudaMemcpyAsync(h, src, n * sizeof(double), cudaMemcpyDeviceToHost, st_));
     } else {
@@ -417,159 +498,177 @@ class Solver : public SolverBase {
     CK(cudaStreamSynchronize(st_));
   }
 
-  void init_ic(uint64_t seed) override {
-    const long long n = nfield_;
-    k_ic<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_, seed);
-    post();
+  void init_ic(int id, uint64_t seed) override {
+    const int slot = slot_of(id);
+    slots_[slot].spec.seed = seed;
+    ic_slot(slot, seed);
     CK(cudaStreamSynchronize(st_));
   }
 
-  // ---------------- stage entry points ------------------------------------
+  // ---------------- stage entry points (all active instances) -----------------
   void filt_da(int f, int fx, int fy) override {
+    need_active();
     const R sc = (R)(1.0 / ((double)d_.nx * d_.ny));
-    SrcFields<R, 1> src{{F_[f]}, sc, 1, 1, d_.ld, kp_.plane};
-    xfwd<1>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
-    ypass_lin<1, 3, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+    SrcFields<R, 1> src{{F_[f]}, sc, 1, 1, d_.ld, kp_.plane, imf(d_.nz)};
+    xfwd<1>(src, d_.nx, d_.ny, d_.nz, specA_, px_);
+    ypass_lin<1, 3, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 1, ROW_SAME,
                                         {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}});
-    DstFields<R, 3> dst{{F_[f], F_[fx], F_[fy]}, 1, 1, d_.ld, kp_.plane};
-    xinv<3>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+    DstFields<R, 3> dst{{F_[f], F_[fx], F_[fy]}, 1, 1, d_.ld, kp_.plane, imf(d_.nz)};
+    xinv<3>(dst, specB_, d_.nx, d_.ny, d_.nz, px_);
   }
   void ddxy(int f, int fx, int fy) override {
+    need_active();
     const R sc = (R)(1.0 / ((double)d_.nx * d_.ny));
-    SrcFields<R, 1> src{{F_[f]}, sc, 1, 1, d_.ld, kp_.plane};
-    xfwd<1>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
+    SrcFields<R, 1> src{{F_[f]}, sc, 1, 1, d_.ld, kp_.plane, imf(d_.nz)};
+    xfwd<1>(src, d_.nx, d_.ny, d_.nz, specA_, px_);
     if (fx >= 0 && fy >= 0) {
-      ypass_lin<1, 2, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+      ypass_lin<1, 2, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 1, ROW_SAME,
                                           {{MUL_IKX}, {MUL_IKY}});
-      DstFields<R, 2> dst{{F_[fx], F_[fy]}, 1, 1, d_.ld, kp_.plane};
-      xinv<2>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+      DstFields<R, 2> dst{{F_[fx], F_[fy]}, 1, 1, d_.ld, kp_.plane, imf(d_.nz)};
+      xinv<2>(dst, specB_, d_.nx, d_.ny, d_.nz, px_);
     } else {
-      ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+      ypass_lin<1, 1, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 1, ROW_SAME,
                                           {{fx >= 0 ? MUL_IKX : MUL_IKY}});
-      DstFields<R, 1> dst{{F_[fx >= 0 ? fx : fy]}, 1, 1, d_.ld, kp_.plane};
-      xinv<1>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+      DstFields<R, 1> dst{{F_[fx >= 0 ? fx : fy]}, 1, 1, d_.ld, kp_.plane, imf(d_.nz)};
+      xinv<1>(dst, specB_, d_.nx, d_.ny, d_.nz, px_);
     }
   }
   void ddz(int f, int dfdz, bool uv) override {
-    const long long n = (long long)d_.nx * d_.ny * d_.nz;
+    need_active();
+    const long long n = (long long)d_.nx * d_.ny * d_.nz * kp_.ninst;
     if (uv) k_ddz<R, true><<<grid1(n), 256, 0, st_>>>(F_[f], F_[dfdz], kp_);
     else k_ddz<R, false><<<grid1(n), 256, 0, st_>>>(F_[f], F_[dfdz], kp_);
     post();
   }
   void test_filter(int f, int level) override {
+    need_active();
     if (level < 0 || level > d_.nz) throw Error(LESGO_ERR_ARG, "level");
-    filter_planes(F_[f], F_[f], level, F_[f] + (long long)level * kp_.plane, F_[f] + (long long)level * kp_.plane, 1);
+    // in place: output planes are the level's planes (instance stride = field stride)
+    filter_planes(F_[f], F_[f], level, F_[f] + (long long)level * kp_.plane, F_[f] + (long long)level * kp_.plane,
+                  1, kp_.istride);
   }
   void wallstress() override {
+    need_active();
     wall_planes();
     const int n = d_.nx * d_.ny;
-    k_wall<R><<<(n + 255) / 256, 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], wall_[0], wall_[1], wall_[2], wall_[3],
-                                                F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_DUDZ], F_[LESGO_DVDZ], kp_);
+    k_wall<R><<<dim3((n + 255) / 256, kp_.ninst), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], wall_[0], wall_[1], wall_[2],
+                                                                wall_[3], F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_DUDZ],
+                                                                F_[LESGO_DVDZ], kp_);
     post();
   }
   void sgs_stag() override {
-    const bool cs_fill = (jt_ == 1 && !d_.p.initu);
-    const bool lag = !cs_fill && (jt_ >= d_.p.dyn_init || d_.p.initu) && (jt_total_ % d_.p.cs_count == 0);
-    if (!lag) {
-      column<COL_STORE_S | COL_TAU>(cs_fill);
+    need_active();
+    bool lag_any = false;
+    upload_flags(false, &lag_any);
+    if (!lag_any) {
+      column<COL_STORE_S | COL_TAU>();
     } else {
-      column<COL_STORE_S>(false);
+      column<COL_STORE_S>();
       lagrange();
-      column<COL_READ_S | COL_TAU>(false);
+      column<COL_READ_S | COL_TAU>();
     }
+    commit_lagrange_init();
   }
   void divstress(int which) override {
+    need_active();
     const R sc = (R)(1.0 / ((double)d_.nx * d_.ny));
     const R idz = (R)(1.0 / d_.dz);
+    const InstMap im = imf(d_.nz);
     if (which == 3) {
-      SrcFields<R, 5> src{{F_[LESGO_TXX], F_[LESGO_TXY], F_[LESGO_TYY], F_[LESGO_TXZ], F_[LESGO_TYZ]}, sc, 1, 1, d_.ld, kp_.plane};
-      xfwd<5>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_, "divstress.xfwd");
-      ypass_lin<5, 3, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+      SrcFields<R, 5> src{{F_[LESGO_TXX], F_[LESGO_TXY], F_[LESGO_TYY], F_[LESGO_TXZ], F_[LESGO_TYZ]}, sc, 1, 1, d_.ld,
+                          kp_.plane, im};
+      xfwd<5>(src, d_.nx, d_.ny, d_.nz, specA_, px_, "divstress.xfwd");
+      ypass_lin<5, 3, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 1, ROW_SAME,
                                           {{MUL_IKX, MUL_IKY, 0, 0, 0}, {0, MUL_IKX, MUL_IKY, 0, 0}, {0, 0, 0, MUL_IKX, MUL_IKY}},
                                           "divstress.ypass");
       DstDiv<R, 3> dst{F_[LESGO_DIVTX], F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_TZZ],
-                       idz, d_.ld, d_.nz, kp_.plane};
-      xinv<3>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_, "divstress.xinv", 6);
+                       idz, d_.ld, d_.nz, kp_.plane, im};
+      xinv<3>(dst, specB_, d_.nx, d_.ny, d_.nz, px_, "divstress.xinv", 6);
     } else if (which == 1) {
-      SrcFields<R, 3> src{{F_[LESGO_TXX], F_[LESGO_TXY], F_[LESGO_TYY]}, sc, 1, 1, d_.ld, kp_.plane};
-      xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
-      ypass_lin<3, 2, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+      SrcFields<R, 3> src{{F_[LESGO_TXX], F_[LESGO_TXY], F_[LESGO_TYY]}, sc, 1, 1, d_.ld, kp_.plane, im};
+      xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, px_);
+      ypass_lin<3, 2, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 1, ROW_SAME,
                                           {{MUL_IKX, MUL_IKY, 0}, {0, MUL_IKX, MUL_IKY}});
       DstDiv<R, 1> dst{F_[LESGO_DIVTX], F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_TZZ],
-                       idz, d_.ld, d_.nz, kp_.plane};
-      xinv<2>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+                       idz, d_.ld, d_.nz, kp_.plane, im};
+      xinv<2>(dst, specB_, d_.nx, d_.ny, d_.nz, px_);
     } else {
-      SrcFields<R, 2> src{{F_[LESGO_TXZ], F_[LESGO_TYZ]}, sc, 1, 1, d_.ld, kp_.plane};
-      xfwd<2>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_);
-      ypass_lin<2, 1, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 1, ROW_SAME,
+      SrcFields<R, 2> src{{F_[LESGO_TXZ], F_[LESGO_TYZ]}, sc, 1, 1, d_.ld, kp_.plane, im};
+      xfwd<2>(src, d_.nx, d_.ny, d_.nz, specA_, px_);
+      ypass_lin<2, 1, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 1, ROW_SAME,
                                           {{MUL_IKX, MUL_IKY}});
       DstDiv<R, 2> dst{F_[LESGO_DIVTX], F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_TXZ], F_[LESGO_TYZ], F_[LESGO_TZZ],
-                       idz, d_.ld, d_.nz, kp_.plane};
-      xinv<1>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+                       idz, d_.ld, d_.nz, kp_.plane, im};
+      xinv<1>(dst, specB_, d_.nx, d_.ny, d_.nz, px_);
     }
   }
-  void convec() override { convec_impl(false, false); }
+  void convec() override { need_active(); convec_impl(false); }
   void turbines_forcing() override {
+    need_active();
     if (!kp_.turbines) return;
     turb_impl();
   }
   void begin_step() override {
-    ++jt_; ++jt_total_;
+    need_active();
+    for (auto& sl : slots_) { ++sl.jt; ++sl.jt_total; }
     for (int c = 0; c < 3; ++c)
-      CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c], F_[LESGO_RHSX + c], nfield_ * sizeof(R), cudaMemcpyDeviceToDevice, st_));
+      CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c], F_[LESGO_RHSX + c], kp_.istride * kp_.ninst * sizeof(R),
+                         cudaMemcpyDeviceToDevice, st_));
   }
   void rhs_assemble() override {
-    const long long n = kp_.plane * d_.nz;
+    need_active();
+    const long long n = kp_.plane * d_.nz * kp_.ninst;
     k_rhs_assemble<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_RHSZ], F_[LESGO_DIVTX],
-                                                 F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_FXA], F_[LESGO_FYA], F_[LESGO_FZA], kp_);
+                                                 F_[LESGO_DIVTY], F_[LESGO_DIVTZ], F_[LESGO_FXA], F_[LESGO_FYA],
+                                                 F_[LESGO_FZA], kp_);
     post();
   }
   void ab2() override {
-    if (jt_total_ == 1 && !d_.p.initu)
-      for (int c = 0; c < 3; ++c)
-        CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c], F_[LESGO_RHSX + c], nfield_ * sizeof(R), cudaMemcpyDeviceToDevice, st_));
-    const long long n = kp_.plane * d_.nz;
-    k_ab2<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_RHSZ],
-                                        F_[LESGO_RHSX_F], F_[LESGO_RHSY_F], F_[LESGO_RHSZ_F], kp_);
+    need_active();
+    for (int s = 0; s < (int)slots_.size(); ++s)
+      if (slots_[s].jt_total == 1 && !d_.p.initu)
+        for (int c = 0; c < 3; ++c)
+          CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c] + s * kp_.istride, F_[LESGO_RHSX + c] + s * kp_.istride,
+                             kp_.istride * sizeof(R), cudaMemcpyDeviceToDevice, st_));
+    const long long n = kp_.plane * d_.nz * kp_.ninst;
+    k_ab2<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_RHSX], F_[LESGO_RHSY],
+                                        F_[LESGO_RHSZ], F_[LESGO_RHSX_F], F_[LESGO_RHSY_F], F_[LESGO_RHSZ_F], kp_);
     post();
   }
-  void press_stag_array() override { pressure_impl(false); }
+  void press_stag_array() override { need_active(); pressure_impl(false); }
   void rhs_sub_dp() override {
-    const long long n = kp_.plane * d_.nz;
+    need_active();
+    const long long n = kp_.plane * d_.nz * kp_.ninst;
     k_rhs_sub_dp<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_RHSZ], F_[LESGO_DPDX],
                                                F_[LESGO_DPDY], F_[LESGO_DPDZ], kp_);
     post();
   }
   void project() override {
-    const long long n = (long long)d_.nx * d_.ny * d_.nz;
+    need_active();
+    const long long n = (long long)d_.nx * d_.ny * d_.nz * kp_.ninst;
     k_project<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_DPDZ], F_[LESGO_U], F_[LESGO_V],
                                             F_[LESGO_W], kp_);
     post();
-    k_project_bc<R><<<grid1(kp_.plane), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_);
+    k_project_bc<R><<<grid1(kp_.plane * kp_.ninst), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_);
     post();
   }
 
   // ---------------- fused time loop ------------------------------------------
   void step(int nsteps) override {
+    need_active();
     for (int s = 0; s < nsteps; ++s) {
-      ++jt_; ++jt_total_;
-      const bool inilag = !d_.p.initu;
-      StepKey key;
-      key.euler = (jt_total_ == 1 && !d_.p.initu);
-      key.cs_fill = (jt_ == 1 && inilag);
-      key.lag = !key.cs_fill && (jt_ >= d_.p.dyn_init || d_.p.initu) && (jt_total_ % d_.p.cs_count == 0);
-      key.init_lm = key.lag && inilag && !F_LM_MM_init_ && (jt_ == d_.p.cs_count || jt_ == d_.p.dyn_init);
-      key.init_qn = key.lag && inilag && !F_QN_NN_init_ && (jt_ == d_.p.cs_count || jt_ == d_.p.dyn_init);
-      const bool steady = !key.euler && !key.cs_fill && !key.init_lm && !key.init_qn;
-      const int code = key.code();
-      if (steady && use_graphs_) {
+      for (auto& sl : slots_) { ++sl.jt; ++sl.jt_total; }
+      bool lag_any = false;
+      const bool special = upload_flags(true, &lag_any);
+      const int code = (lag_any ? 1 : 0) | (kp_.ninst << 1);
+      if (!special && use_graphs_) {
         auto it = graphs_.find(code);
         if (it == graphs_.end()) {
           cudaGraph_t g;
           launches_ = 0;
           CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
           try {
-            step_body(key);
+            step_body(lag_any);
           } catch (...) {
             cudaStreamEndCapture(st_, &g);
             throw;
@@ -579,17 +678,16 @@ class Solver : public SolverBase {
           CK(cudaGraphInstantiate(&ge, g, 0));
           cudaGraphDestroy(g);
           graphs_[code] = ge;
-          launch_count_[code] = launches_;
+          launch_count_[lag_any ? 1 : 0] = launches_;
           it = graphs_.find(code);
         }
         CK(cudaGraphLaunch(it->second, st_));
       } else {
         launches_ = 0;
-        step_body(key);
-        launch_count_[code] = launches_;
+        step_body(lag_any);
+        if (!special) launch_count_[lag_any ? 1 : 0] = launches_;
       }
-      if (key.init_lm) F_LM_MM_init_ = true;
-      if (key.init_qn) F_QN_NN_init_ = true;
+      commit_lagrange_init();
     }
   }
 
@@ -604,11 +702,12 @@ class Solver : public SolverBase {
     return LESGO_OK;
   }
 
-  void diag(double* out) override {
+  void diag(int id, double* out) override {
+    const int slot = slot_of(id);
     const int nb = 4 * 152;
     if (!diag_part_) { diag_part_ = alloc<double>(nb * 7); diag_out_ = alloc<double>(8); }
     k_diag<R><<<nb, 256, 0, st_>>>(F_[LESGO_DUDX], F_[LESGO_DVDY], F_[LESGO_DWDZ], F_[LESGO_U], F_[LESGO_V], F_[LESGO_W],
-                                   F_[LESGO_TXZ], F_[LESGO_TYZ], kp_, diag_part_);
+                                   F_[LESGO_TXZ], F_[LESGO_TYZ], kp_, diag_part_, slot);
     post();
     k_diag_final<<<1, 32, 0, st_>>>(diag_part_, nb, diag_out_);
     post();
@@ -623,24 +722,34 @@ class Solver : public SolverBase {
     out[3] = std::sqrt((h[5] / nxy) * (h[5] / nxy) + (h[6] / nxy) * (h[6] / nxy));
   }
 
-  void counters(int* jt, int* jt_total) const override {
-    if (jt) *jt = jt_;
-    if (jt_total) *jt_total = jt_total_;
+  void counters(int id, int* jt, int* jt_total) const override {
+    const Slot& sl = slots_[slot_of(id)];
+    if (jt) *jt = sl.jt;
+    if (jt_total) *jt_total = sl.jt_total;
   }
 
-  void turbine_state(double* udT, double* fn, double* pw, int n) override {
-    const int m = std::min(n, th_.n);
-    std::vector<double> a(th_.n), b(th_.n);
+  void turbine_state(int id, double* udT, double* fn, double* pw, int n) override {
+    const int slot = slot_of(id);
+    int first = 0;
+    for (int s = 0; s < slot; ++s) first += (int)slots_[s].spec.turbines.size();
+    const int nt = (int)slots_[slot].spec.turbines.size();
+    const int m = std::min(n, nt);
+    std::vector<double> a(std::max(th_.n, 1)), b(std::max(th_.n, 1));
     if (th_.n) {
       CK(cudaStreamSynchronize(st_));
       CK(cudaMemcpy(a.data(), td_.u_d_T, th_.n * sizeof(double), cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(b.data(), td_.f_n, th_.n * sizeof(double), cudaMemcpyDeviceToHost));
     }
     for (int s = 0; s < m; ++s) {
-      if (udT) udT[s] = a[s];
-      if (fn) fn[s] = b[s];
-      if (pw) pw[s] = -b[s] * a[s];
+      if (udT) udT[s] = a[first + s];
+      if (fn) fn[s] = b[first + s];
+      if (pw) pw[s] = -b[first + s] * a[first + s];
     }
+  }
+
+  int launches_per_step(int with_sgs) const override {
+    auto it = launch_count_.find(with_sgs ? 1 : 0);
+    return it == launch_count_.end() ? -1 : it->second;
   }
 
   // Profiling: eager steps with an event pair per launch; the report is a
@@ -699,48 +808,150 @@ class Solver : public SolverBase {
     return LESGO_OK;
   }
 
-  int launches_per_step(int with_sgs) const override {
-    for (auto& kv : launch_count_) {
-      StepKey k = StepKey::from(kv.first);
-      if (k.lag == (with_sgs != 0) && !k.euler && !k.cs_fill && !k.init_lm && !k.init_qn) return kv.second;
-    }
-    return -1;
-  }
-
  private:
-  struct StepKey {
-    bool euler = false, cs_fill = false, lag = false, init_lm = false, init_qn = false;
-    int code() const { return euler | (cs_fill << 1) | (lag << 2) | (init_lm << 3) | (init_qn << 4); }
-    static StepKey from(int c) {
-      StepKey k;
-      k.euler = c & 1; k.cs_fill = c & 2; k.lag = c & 4; k.init_lm = c & 8; k.init_qn = c & 16;
-      return k;
-    }
+  struct Slot {
+    int id = -1;
+    InstanceSpec spec;
+    int jt = 0, jt_total = 0;
+    bool flm_init = false, fqn_init = false;
+    int pending = 0;   // IF_INITLM / IF_INITQN set this step (committed after it)
   };
 
-  void step_body(const StepKey& key) {
+  int slot_of(int id) const {
+    for (int s = 0; s < (int)slots_.size(); ++s)
+      if (slots_[s].id == id) return s;
+    throw Error(LESGO_ERR_ARG, "unknown instance id " + std::to_string(id));
+  }
+  void need_active() const {
+    if (slots_.empty()) throw Error(LESGO_ERR_ARG, "no active instance");
+  }
+  InstMap imf(int nli) const { return InstMap{nli, kp_.istride}; }
+
+  void sync_instance_params() {
+    kp_.ninst = (int)slots_.size();
+    std::vector<double> zo(cap_, d_.p.zo);
+    for (size_t s = 0; s < slots_.size(); ++s) zo[s] = slots_[s].spec.zo;
+    CK(cudaMemcpyAsync(zo_d_, zo.data(), cap_ * sizeof(double), cudaMemcpyHostToDevice, st_));
+    CK(cudaStreamSynchronize(st_));
+  }
+
+  // Per-instance flags of this step (counters already advanced).  Returns
+  // true when some flag other than IF_LAG is set (a step that is not replayed).
+  bool upload_flags(bool count_euler, bool* lag_any) {
+    const bool inilag = !d_.p.initu;
+    std::vector<int> fl(slots_.size(), 0);
+    bool special = false, lag = false;
+    for (size_t s = 0; s < slots_.size(); ++s) {
+      Slot& sl = slots_[s];
+      int f = 0;
+      if (count_euler && sl.jt_total == 1 && !d_.p.initu) f |= IF_EULER;
+      const bool cs_fill = (sl.jt == 1 && inilag);
+      if (cs_fill) f |= IF_CSFILL;
+      if (!cs_fill && (sl.jt >= d_.p.dyn_init || d_.p.initu) && (sl.jt_total % d_.p.cs_count == 0)) {
+        f |= IF_LAG;
+        if (inilag && !sl.flm_init && (sl.jt == d_.p.cs_count || sl.jt == d_.p.dyn_init)) f |= IF_INITLM;
+        if (inilag && !sl.fqn_init && (sl.jt == d_.p.cs_count || sl.jt == d_.p.dyn_init)) f |= IF_INITQN;
+      }
+      sl.pending = f & (IF_INITLM | IF_INITQN);
+      if (f & ~IF_LAG) special = true;
+      if (f & IF_LAG) lag = true;
+      fl[s] = f;
+    }
+    CK(cudaMemcpyAsync(flags_d_, fl.data(), fl.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
+    *lag_any = lag;
+    return special;
+  }
+  void commit_lagrange_init() {
+    for (auto& sl : slots_) {
+      if (sl.pending & IF_INITLM) sl.flm_init = true;
+      if (sl.pending & IF_INITQN) sl.fqn_init = true;
+      sl.pending = 0;
+    }
+  }
+
+  void ic_slot(int slot, uint64_t seed) {
+    const long long n = kp_.istride;
+    k_ic<R><<<grid1(n), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_, seed, slot);
+    post();
+  }
+
+  void rebuild_turbines(int moved_to, int moved_from) {
+    // carry the disk-velocity state (u_d_T) of surviving turbines across the rebuild
+    std::vector<double> old(std::max(th_.n, 1), -1.0);
+    if (th_.n) CK(cudaMemcpy(old.data(), td_.u_d_T, th_.n * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<std::vector<lesgo_turbine_t>> per;
+    for (auto& sl : slots_) per.push_back(sl.spec.turbines);
+    std::vector<double> state;
+    for (size_t s = 0; s < slots_.size(); ++s) {
+      const int id = slots_[s].id;
+      auto it = turb_base_.find(id);
+      for (size_t t = 0; t < slots_[s].spec.turbines.size(); ++t)
+        state.push_back(it != turb_base_.end() && it->second + (int)t < (int)old.size() && th_.n ? old[it->second + t] : -1.0);
+    }
+    th_ = turbines_build(d_, per, kp_.istride, ind_cache_);
+    turb_base_.clear();
+    int base = 0;
+    for (auto& sl : slots_) { turb_base_[sl.id] = base; base += (int)sl.spec.turbines.size(); }
+    kp_.turbines = th_.n > 0 ? 1 : 0;
+    if (!kp_.turbines) return;
+    if (!fza_uv_) fza_uv_ = alloc<R>(nfield_);
+    td_.nturb = th_.n;
+    td_.node_off = upload_vec(th_.node_off);
+    td_.node_q = upload_vec(th_.node_q);
+    td_.node_ind = upload_vec(th_.node_ind);
+    td_.win_turb = upload_vec(th_.win_turb);
+    td_.win_q = upload_vec(th_.win_q);
+    td_.win_ind = upload_vec(th_.win_ind);
+    td_.nwin = (int)th_.win_q.size();
+    td_.nhat = upload_vec(th_.nhat);
+    td_.ctp = upload_vec(th_.ctp);
+    td_.corr = upload_vec(th_.corr);
+    td_.dia = upload_vec(th_.dia);
+    td_.u_d = alloc<double>(th_.n);
+    td_.u_d_T = upload_vec(state);
+    td_.f_n = alloc<double>(th_.n);
+    td_.disk = alloc<double>(th_.n);
+    const double dt_dim = d_.p.dt * d_.p.z_i / d_.p.u_star;
+    td_.eps = d_.p.T_avg_dim > 0 ? (dt_dim / d_.p.T_avg_dim) / (1. + dt_dim / d_.p.T_avg_dim) : 1.0;
+    td_.dvol = d_.dx * d_.dy * d_.dz;
+    cols_ = upload_vec(th_.cols);
+    // the applied-force fields are rewritten only on disk nodes: clear them
+    for (int f : {LESGO_FXA, LESGO_FYA, LESGO_FZA})
+      CK(cudaMemsetAsync(F_[f], 0, nfield_ * sizeof(R), st_));
+    CK(cudaMemsetAsync(fza_uv_, 0, nfield_ * sizeof(R), st_));
+    graphs_clear();
+    (void)moved_to; (void)moved_from;
+  }
+  void graphs_clear() {
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+  }
+
+  void step_body(bool lag_any) {
     // main.f90:155-172: derivatives (RHS_f is saved inside the fused convec epilogue)
-    SrcFields<R, 3> src{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, (R)(1.0 / ((double)d_.nx * d_.ny)), 1, 1, d_.ld, kp_.plane};
-    xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_, "filt_da.xfwd");
-    ypass_lin<1, 3, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 3, ROW_SAME,
+    const InstMap im = imf(d_.nz);
+    SrcFields<R, 3> src{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, (R)(1.0 / ((double)d_.nx * d_.ny)), 1, 1, d_.ld,
+                        kp_.plane, im};
+    xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, px_, "filt_da.xfwd");
+    ypass_lin<1, 3, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 3, ROW_SAME,
                                         {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}}, "filt_da.ypass");
     DstFields<R, 9> dst{{F_[LESGO_U], F_[LESGO_DUDX], F_[LESGO_DUDY], F_[LESGO_V], F_[LESGO_DVDX], F_[LESGO_DVDY],
-                         F_[LESGO_W], F_[LESGO_DWDX], F_[LESGO_DWDY]}, 1, 1, d_.ld, kp_.plane};
-    xinv<9>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_, "filt_da.xinv");
+                         F_[LESGO_W], F_[LESGO_DWDX], F_[LESGO_DWDY]}, 1, 1, d_.ld, kp_.plane, im};
+    xinv<9>(dst, specB_, d_.nx, d_.ny, d_.nz, px_, "filt_da.xinv");
     // wall model inputs (test-filtered first level), main.f90:180-189
     wall_planes();
     // applied forcing uses the filtered velocity of this step (main.f90:248-257)
     if (kp_.turbines) turb_impl();
     // sgs_stag with ddz_uv/ddz_w and the wall values fused (main.f90:164-189)
-    if (!key.lag) {
-      column<COL_DDZ | COL_TAU>(key.cs_fill);
+    if (!lag_any) {
+      column<COL_DDZ | COL_TAU>();
     } else {
-      column<COL_DDZ | COL_STORE_S>(false);
-      lagrange(key.init_lm, key.init_qn);
-      column<COL_READ_S | COL_TAU>(false);
+      column<COL_DDZ | COL_STORE_S>();
+      lagrange();
+      column<COL_READ_S | COL_TAU>();
     }
     divstress(3);
-    convec_impl(true, key.euler);
+    convec_impl(true);
     pressure_impl(true);
   }
 
@@ -755,8 +966,8 @@ class Solver : public SolverBase {
   }
   double* staging(long long n) {
     if (n > staging_n_) {
-      staging_ = alloc<double>(nfield_);
-      staging_n_ = nfield_;
+      staging_ = alloc<double>(kp_.istride);
+      staging_n_ = kp_.istride;
     }
     return staging_;
   }
@@ -874,38 +1085,16 @@ class Solver : public SolverBase {
     return p;
   }
 
-  void build_turbines() {
-    th_ = turbines_init_host(d_);
-    td_.nturb = th_.n;
-    td_.node_off = upload_vec(th_.node_off);
-    td_.node_q = upload_vec(th_.node_q);
-    td_.node_ind = upload_vec(th_.node_ind);
-    td_.win_turb = upload_vec(th_.win_turb);
-    td_.win_q = upload_vec(th_.win_q);
-    td_.win_ind = upload_vec(th_.win_ind);
-    td_.nwin = (int)th_.win_q.size();
-    td_.nhat = upload_vec(th_.nhat);
-    td_.ctp = upload_vec(th_.ctp);
-    td_.corr = upload_vec(th_.corr);
-    td_.dia = upload_vec(th_.dia);
-    td_.u_d = alloc<double>(th_.n);
-    td_.u_d_T = upload_vec(std::vector<double>(th_.n, d_.p.n_turbines ? -1.0 : 0.0));
-    td_.f_n = alloc<double>(th_.n);
-    td_.disk = alloc<double>(th_.n);
-    const double dt_dim = d_.p.dt * d_.p.z_i / d_.p.u_star;
-    td_.eps = d_.p.T_avg_dim > 0 ? (dt_dim / d_.p.T_avg_dim) / (1. + dt_dim / d_.p.T_avg_dim) : 1.0;
-    td_.dvol = d_.dx * d_.dy * d_.dz;
-    cols_ = upload_vec(th_.cols);
-  }
-
+  // Batched passes over nli levels of every active instance.  Spectral
+  // buffers hold [field][instance*nli + level][row][kx].
   template <int NF, class Src>
-  void xfwd(const Src& src, int M, int nyrows, int nlev, T2* out, long long out_fs, const FftPlan<R>& plan,
-            const char* tag = "xfwd", int in_fields = NF) {
+  void xfwd(const Src& src, int M, int nyrows, int nli, T2* out, const FftPlan<R>& plan, const char* tag = "xfwd",
+            int in_fields = NF) {
     XfGeom g;
-    g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nlev; g.ls = M / 2 + 1;
+    g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nli * kp_.ninst; g.ls = M / 2 + 1;
     const int target = sizeof(R) == 8 ? 2048 : 4096;
     g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
-    g.out_field_stride = out_fs;
+    g.out_field_stride = (long long)g.nrows * g.K;
     const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
     auto kern = k_xfwd<R, NF, Src>;
     set_smem(kern, smem);
@@ -915,13 +1104,13 @@ class Solver : public SolverBase {
   }
 
   template <int NF, class Dst>
-  void xinv(const Dst& dst, const T2* in, long long in_fs, int M, int nyrows, int nlev, const FftPlan<R>& plan,
-            const char* tag = "xinv", int out_fields = NF) {
+  void xinv(const Dst& dst, const T2* in, int M, int nyrows, int nli, const FftPlan<R>& plan, const char* tag = "xinv",
+            int out_fields = NF) {
     XiGeom g;
-    g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nlev; g.ls = M / 2 + 1;
+    g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nli * kp_.ninst; g.ls = M / 2 + 1;
     const int target = sizeof(R) == 8 ? 2048 : 4096;
     g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
-    g.in_field_stride = in_fs;
+    g.in_field_stride = (long long)g.nrows * g.K;
     const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
     auto kern = k_xinv<R, NF, Dst>;
     set_smem(kern, smem);
@@ -930,14 +1119,20 @@ class Solver : public SolverBase {
     post(tag, (double)g.nrows * ((double)NF * g.K * sizeof(T2) + (double)out_fields * M * sizeof(R)));
   }
 
-  // Y pass over groups of NIN inputs -> NOUT outputs.
+  // Y pass over groups of NIN inputs -> NOUT outputs, nli levels of every
+  // instance.  Input field g*NIN+i holds in_inst_levels planes per instance
+  // (read at in_lev0 + level*in_levstride); outputs are contiguous.
   template <int NIN, int NOUT, bool FWD, bool INV, typename InT, typename OutT>
-  void ypass_lin(const InT* in, long long in_fs, int in_lev0, int in_levstride, int in_rows, OutT* out, long long out_fs,
-                 int out_rows, int nlev, int ngroups, int rowmode, std::initializer_list<std::initializer_list<int>> mul,
+  void ypass_lin(const InT* in, int in_lev0, int in_levstride, int in_inst_levels, int in_rows, OutT* out,
+                 int out_rows, int nli, int ngroups, int rowmode, std::initializer_list<std::initializer_list<int>> mul,
                  const char* tag = "ypass") {
+    const int nlev = nli * kp_.ninst;
     YOpLin<R, NIN, NOUT, InT, OutT> op;
-    op.in = in; op.in_fs = in_fs; op.in_lev0 = in_lev0; op.in_levstride = in_levstride; op.in_rows = in_rows;
-    op.out = out; op.out_fs = out_fs; op.out_rows = out_rows;
+    op.in = in;
+    op.in_fs = (long long)in_inst_levels * kp_.ninst * in_rows * d_.K;
+    op.in_lev0 = in_lev0; op.in_levstride = in_levstride; op.in_rows = in_rows;
+    op.nli = nli; op.in_inst_levels = in_inst_levels;
+    op.out = out; op.out_fs = (long long)nlev * out_rows * d_.K; op.out_rows = out_rows;
     op.K = d_.K; op.lh = d_.lh; op.ny_small = d_.ny; op.ny_big = d_.ny2; op.rowmode = rowmode;
     int o = 0;
     for (auto& row : mul) {
@@ -972,27 +1167,30 @@ class Solver : public SolverBase {
                   ((double)NIN * in_rows * sizeof(InT) + (double)NOUT * out_rows * sizeof(OutT)));
   }
 
-  // test-filter (G_test) of one plane of two fields into two (ld, ny) planes
-  void filter_planes(const R* a, const R* b, int level, R* oa, R* ob, int nf) {
-    SrcFields<R, 2> src{{a, b}, (R)1, level, 1, d_.ld, kp_.plane};
-    xfwd<2>(src, d_.nx, d_.ny, 1, specC_, (long long)d_.ny * d_.K, px_, "wall_filter.xfwd");
-    ypass_lin<1, 1, true, true, T2, T2>(specC_, (long long)d_.ny * d_.K, 0, 1, d_.ny, specC_ + 2LL * d_.ny * d_.K,
-                                        (long long)d_.ny * d_.K, d_.ny, 1, 2, ROW_SAME, {{MUL_G1}}, "wall_filter.ypass");
+  // test filter (G_test) of plane `level` of two fields into two planes per
+  // instance (out planes are `ostr` apart between instances)
+  void filter_planes(const R* a, const R* b, int level, R* oa, R* ob, int nf, long long ostr) {
+    const long long pl_s = (long long)d_.ny * d_.K;
+    T2* in = specC_;
+    T2* outp = specC_ + 2 * pl_s * kp_.ninst;
+    SrcFields<R, 2> src{{a, b}, (R)1, level, 1, d_.ld, kp_.plane, imf(1)};
+    xfwd<2>(src, d_.nx, d_.ny, 1, in, px_, "wall_filter.xfwd");
+    ypass_lin<1, 1, true, true, T2, T2>(in, 0, 1, 1, d_.ny, outp, d_.ny, 1, 2, ROW_SAME, {{MUL_G1}}, "wall_filter.ypass");
     if (nf == 1) {
-      DstFields<R, 1> dst{{oa}, 0, 1, d_.ld, 0};
-      xinv<1>(dst, specC_ + 2LL * d_.ny * d_.K, (long long)d_.ny * d_.K, d_.nx, d_.ny, 1, px_, "wall_filter.xinv");
+      DstFields<R, 1> dst{{oa}, 0, 1, d_.ld, 0, InstMap{1, ostr}};
+      xinv<1>(dst, outp, d_.nx, d_.ny, 1, px_, "wall_filter.xinv");
     } else {
-      DstFields<R, 2> dst{{oa, ob}, 0, 1, d_.ld, 0};
-      xinv<2>(dst, specC_ + 2LL * d_.ny * d_.K, (long long)d_.ny * d_.K, d_.nx, d_.ny, 1, px_, "wall_filter.xinv");
+      DstFields<R, 2> dst{{oa, ob}, 0, 1, d_.ld, 0, InstMap{1, ostr}};
+      xinv<2>(dst, outp, d_.nx, d_.ny, 1, px_, "wall_filter.xinv");
     }
   }
   void wall_planes() {
-    if (d_.p.lbc_mom == 2) filter_planes(F_[LESGO_U], F_[LESGO_V], 1, wall_[0], wall_[1], 2);
-    if (d_.p.ubc_mom == 2) filter_planes(F_[LESGO_U], F_[LESGO_V], d_.nz - 1, wall_[2], wall_[3], 2);
+    if (d_.p.lbc_mom == 2) filter_planes(F_[LESGO_U], F_[LESGO_V], 1, wall_[0], wall_[1], 2, kp_.plane);
+    if (d_.p.ubc_mom == 2) filter_planes(F_[LESGO_U], F_[LESGO_V], d_.nz - 1, wall_[2], wall_[3], 2, kp_.plane);
   }
 
   template <int FLAGS>
-  void column(bool cs_fill) {
+  void column() {
     ColArgs<R> a;
     a.u = F_[LESGO_U]; a.v = F_[LESGO_V]; a.w = F_[LESGO_W];
     a.dudx = F_[LESGO_DUDX]; a.dudy = F_[LESGO_DUDY]; a.dvdx = F_[LESGO_DVDX]; a.dvdy = F_[LESGO_DVDY];
@@ -1007,34 +1205,30 @@ class Solver : public SolverBase {
     a.kp = kp_;
     a.delta2 = d_.delta * d_.delta;
     a.chunk = 16;
-    a.cs_fill = cs_fill ? 1 : 0;
     const int ncol = d_.nx * d_.ny;
-    dim3 grid((ncol + 255) / 256, (d_.nz + a.chunk - 1) / a.chunk);
+    dim3 grid((ncol + 255) / 256, (d_.nz + a.chunk - 1) / a.chunk, kp_.ninst);
     const int nrw = (FLAGS & COL_READ_S) ? 13 : (FLAGS & COL_TAU) ? 19 : 18;
     pre();
     k_column<R, FLAGS><<<grid, 256, 0, st_>>>(a);
     post((FLAGS & COL_READ_S) ? "sgs_column.tau" : (FLAGS & COL_TAU) ? "sgs_column" : "sgs_column.sij",
-         (double)nrw * ncol * d_.nz * sizeof(R));
-    if (cs_fill && !(FLAGS & COL_TAU)) {
-      k_fill<R><<<grid1(nfield_), 256, 0, st_>>>(F_[LESGO_CS_OPT2], nfield_, (R)0.03);
-      post();
-    }
+         (double)nrw * ncol * d_.nz * kp_.ninst * sizeof(R));
   }
 
-  void lagrange(bool init_lm, bool init_qn) {
+  void lagrange() {
     InterpArgs<R> ia;
     ia.u = F_[LESGO_U]; ia.v = F_[LESGO_V]; ia.w = F_[LESGO_W];
     const int Fi[4] = {LESGO_F_LM, LESGO_F_MM, LESGO_F_QN, LESGO_F_NN};
     for (int f = 0; f < 4; ++f) { ia.Fin[f] = F_[Fi[f]]; ia.Fout[f] = Ftmp_[f]; }
     ia.kp = kp_;
-    const long long n = (long long)d_.nx * d_.ny * d_.nz;
+    const long long n = (long long)d_.nx * d_.ny * d_.nz * kp_.ninst;
     pre();
     k_interp<R><<<grid1(n), 256, 0, st_>>>(ia);
     post("lagrange.interp", 11.0 * n * sizeof(R));
     SrcLagrange<R> src{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_S11], F_[LESGO_S12], F_[LESGO_S13],
-                       F_[LESGO_S22], F_[LESGO_S23], F_[LESGO_S33], d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane};
-    xfwd<21>(src, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_, "lagrange.xfwd", 9);
-    ypass_lin<1, 2, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_s_, d_.ny, d_.nz, 21, ROW_SAME,
+                       F_[LESGO_S22], F_[LESGO_S23], F_[LESGO_S33], d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane,
+                       imf(d_.nz)};
+    xfwd<21>(src, d_.nx, d_.ny, d_.nz, specA_, px_, "lagrange.xfwd", 9);
+    ypass_lin<1, 2, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 21, ROW_SAME,
                                         {{MUL_G1}, {MUL_G2}}, "lagrange.ypass");
     DstLagrange<R> dst;
     dst.FLMi = Ftmp_[0]; dst.FMMi = Ftmp_[1]; dst.FQNi = Ftmp_[2]; dst.FNNi = Ftmp_[3];
@@ -1045,38 +1239,33 @@ class Solver : public SolverBase {
     dst.lagran_dt = d_.lagran_dt;
     dst.beta_exp = std::log(2.0) / (std::log(4.0) - std::log(2.0));
     dst.ld = d_.ld; dst.nz = d_.nz; dst.lbc = kp_.lbc; dst.ubc = kp_.ubc;
-    dst.init_lm = init_lm; dst.init_qn = init_qn;
+    dst.iflags = flags_d_;
     dst.plane = kp_.plane;
-    xinv<42>(dst, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_, "lagrange.xinv", 13);
-  }
-  void lagrange() {
-    const bool inilag = !d_.p.initu;
-    const bool init_lm = inilag && !F_LM_MM_init_ && (jt_ == d_.p.cs_count || jt_ == d_.p.dyn_init);
-    const bool init_qn = inilag && !F_QN_NN_init_ && (jt_ == d_.p.cs_count || jt_ == d_.p.dyn_init);
-    lagrange(init_lm, init_qn);
-    if (init_lm) F_LM_MM_init_ = true;
-    if (init_qn) F_QN_NN_init_ = true;
+    dst.im = imf(d_.nz);
+    xinv<42>(dst, specB_, d_.nx, d_.ny, d_.nz, px_, "lagrange.xinv", 13);
   }
 
-  void convec_impl(bool fused, bool euler) {
+  void convec_impl(bool fused) {
     const R c = (R)(1.0 / ((double)d_.nx * d_.ny));
+    const InstMap im = imf(d_.nz);
+    const InstMap imb{d_.nz, kp_.istride_big};
     SrcVort<R> sv{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDY], F_[LESGO_DUDZ], F_[LESGO_DVDX],
-                  F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane};
-    xfwd<6>(sv, d_.nx, d_.ny, d_.nz, specA_, vol_s_, px_, "convec.xfwd", 9);
-    ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_s_, 0, 1, d_.ny, specB_, vol_b_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}},
+                  F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane, im};
+    xfwd<6>(sv, d_.nx, d_.ny, d_.nz, specA_, px_, "convec.xfwd", 9);
+    ypass_lin<1, 1, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}},
                                         "convec.ypass_pad");
-    DstFields<R, 6> db{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld_big, kp_.plane_big};
-    xinv<6>(db, specB_, vol_b_, d_.nx2, d_.ny2, d_.nz, pxb_, "convec.xinv_big");
+    DstFields<R, 6> db{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld_big, kp_.plane_big, imb};
+    xinv<6>(db, specB_, d_.nx2, d_.ny2, d_.nz, pxb_, "convec.xinv_big");
     const R cb = (R)(1.0 / ((double)d_.nx2 * d_.ny2));
-    SrcConvProd<R> sp{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5], cb, d_.ld_big, d_.nz, kp_.plane_big};
-    xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, specA_, vol_b_, pxb_, "convec.xfwd_big", 6);
-    ypass_lin<1, 1, true, true, T2, T2>(specA_, vol_b_, 0, 1, d_.ny2, specB_, vol_s_, d_.ny, d_.nz, 3, ROW_UNPAD, {{MUL_ONE}},
+    SrcConvProd<R> sp{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5], cb, d_.ld_big, d_.nz, kp_.plane_big, imb};
+    xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, specA_, pxb_, "convec.xfwd_big", 6);
+    ypass_lin<1, 1, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny2, specB_, d_.ny, d_.nz, 3, ROW_UNPAD, {{MUL_ONE}},
                                         "convec.ypass_unpad");
     if (!fused) {
       DstConvec<R, false> dc{};
       dc.RHSx = F_[LESGO_RHSX]; dc.RHSy = F_[LESGO_RHSY]; dc.RHSz = F_[LESGO_RHSZ];
-      dc.ld = d_.ld; dc.nz = d_.nz; dc.plane = kp_.plane;
-      xinv<3>(dc, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_);
+      dc.ld = d_.ld; dc.nz = d_.nz; dc.plane = kp_.plane; dc.iflags = flags_d_; dc.im = im;
+      xinv<3>(dc, specB_, d_.nx, d_.ny, d_.nz, px_);
     } else {
       DstConvec<R, true> dc{};
       dc.RHSx = F_[LESGO_RHSX]; dc.RHSy = F_[LESGO_RHSY]; dc.RHSz = F_[LESGO_RHSZ];
@@ -1085,9 +1274,9 @@ class Solver : public SolverBase {
       dc.divtx = F_[LESGO_DIVTX]; dc.divty = F_[LESGO_DIVTY]; dc.divtz = F_[LESGO_DIVTZ];
       dc.fxa = F_[LESGO_FXA]; dc.fya = F_[LESGO_FYA]; dc.fza = F_[LESGO_FZA];
       dc.dt = d_.p.dt; dc.t1 = d_.tadv1; dc.t2 = d_.tadv2; dc.mpfx = d_.mpfx; dc.mpfy = d_.mpfy;
-      dc.ld = d_.ld; dc.nz = d_.nz; dc.euler = euler ? 1 : 0; dc.use_mpf = d_.p.use_mean_p_force; dc.turbines = kp_.turbines;
-      dc.plane = kp_.plane;
-      xinv<3>(dc, specB_, vol_s_, d_.nx, d_.ny, d_.nz, px_, "convec.xinv_ab2", 18 + 3 * kp_.turbines);
+      dc.ld = d_.ld; dc.nz = d_.nz; dc.use_mpf = d_.p.use_mean_p_force; dc.turbines = kp_.turbines;
+      dc.iflags = flags_d_; dc.plane = kp_.plane; dc.im = im;
+      xinv<3>(dc, specB_, d_.nx, d_.ny, d_.nz, px_, "convec.xinv_ab2", 18 + 3 * kp_.turbines);
     }
   }
 
@@ -1096,40 +1285,41 @@ class Solver : public SolverBase {
     const long long pl_s = (long long)ny * d_.K;
     const double c1 = 1.0 / ((double)d_.nx * d_.ny);
     const R c2 = (R)(c1 / d_.tadv1 / d_.p.dt);
-    SrcFields<R, 3> su{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, c2, 1, 1, d_.ld, kp_.plane};
-    xfwd<3>(su, d_.nx, ny, nz, specA_, vol_s_, px_, "press.xfwd");
-    SrcFields<R, 1> sd{{F_[LESGO_DIVTZ]}, (R)c1, 1, nz - 1, d_.ld, kp_.plane};
-    xfwd<1>(sd, d_.nx, ny, 2, specC_, 2 * pl_s, px_, "press.xfwd_bc");
-    ypass_lin<1, 1, true, false, T2, double2>(specA_, vol_s_, 0, 1, ny, hspec_, vol_s_, ny, nz, 3, ROW_SAME, {{MUL_ONE}},
+    SrcFields<R, 3> su{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, c2, 1, 1, d_.ld, kp_.plane, imf(nz)};
+    xfwd<3>(su, d_.nx, ny, nz, specA_, px_, "press.xfwd");
+    SrcFields<R, 1> sd{{F_[LESGO_DIVTZ]}, (R)c1, 1, nz - 1, d_.ld, kp_.plane, imf(2)};
+    xfwd<1>(sd, d_.nx, ny, 2, specC_, px_, "press.xfwd_bc");
+    ypass_lin<1, 1, true, false, T2, double2>(specA_, 0, 1, nz, ny, hspec_, ny, nz, 3, ROW_SAME, {{MUL_ONE}},
                                               "press.ypass_fwd");
-    ypass_lin<1, 1, true, false, T2, double2>(specC_, 2 * pl_s, 0, 1, ny, hplane_, 2 * pl_s, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
+    ypass_lin<1, 1, true, false, T2, double2>(specC_, 0, 1, 2, ny, hplane_, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
                                               "press.ypass_fwd_bc");
+    const long long vs = vol1_s_ * kp_.ninst;
     ThomasArgs ta;
-    ta.Hx = hspec_; ta.Hy = hspec_ + vol_s_; ta.Hz = hspec_ + 2 * vol_s_;
+    ta.Hx = hspec_; ta.Hy = hspec_ + vs; ta.Hz = hspec_ + 2 * vs;
     ta.Hb = hplane_; ta.Ht = hplane_ + pl_s;
     ta.phat = phat_; ta.gam = gam_;
     ta.kxw = kxw64_; ta.kyw = kyw64_;
-    ta.dz = d_.dz; ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.err = err_;
+    ta.dz = d_.dz; ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.ninst = kp_.ninst; ta.err = err_;
     pre();
-    k_thomas<<<(unsigned)((pl_s + 127) / 128), 128, 0, st_>>>(ta);
-    post("press.thomas", (double)pl_s * (4.0 * nz + 1.0) * sizeof(double2));
-    // p, i kx p, i ky p at levels 1..nz-1; p at levels 0 and nz
-    ypass_lin<1, 3, false, true, double2, T2>(phat_, 0, 1, 1, ny, specB_, vol_s_, ny, nz - 1, 1, ROW_SAME,
+    k_thomas<<<(unsigned)((pl_s * kp_.ninst + 127) / 128), 128, 0, st_>>>(ta);
+    post("press.thomas", (double)pl_s * kp_.ninst * (4.0 * nz + 1.0) * sizeof(double2));
+    // p, i kx p, i ky p at levels 1..nz-1; p at levels 0 and nz (phat holds nz+1 planes per instance)
+    ypass_lin<1, 3, false, true, double2, T2>(phat_, 1, 1, nz + 1, ny, specB_, ny, nz - 1, 1, ROW_SAME,
                                               {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}}, "press.ypass_inv");
-    ypass_lin<1, 1, false, true, double2, T2>(phat_, 0, 0, nz, ny, specC_, 2 * pl_s, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
+    ypass_lin<1, 1, false, true, double2, T2>(phat_, 0, nz, nz + 1, ny, specC_, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
                                               "press.ypass_inv_bc");
     if (fused) {
-      DstPress<R, true> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U], F_[LESGO_V],
-                           d_.p.dt, d_.tadv1, d_.ld, kp_.plane};
-      xinv<3>(dp, specB_, vol_s_, d_.nx, ny, nz - 1, px_, "press.xinv_project", 9);
+      DstPress<R, true> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U],
+                           F_[LESGO_V], d_.p.dt, d_.tadv1, d_.ld, kp_.plane, imf(nz - 1)};
+      xinv<3>(dp, specB_, d_.nx, ny, nz - 1, px_, "press.xinv_project", 9);
     } else {
-      DstPress<R, false> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U], F_[LESGO_V],
-                            d_.p.dt, d_.tadv1, d_.ld, kp_.plane};
-      xinv<3>(dp, specB_, vol_s_, d_.nx, ny, nz - 1, px_);
+      DstPress<R, false> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U],
+                            F_[LESGO_V], d_.p.dt, d_.tadv1, d_.ld, kp_.plane, imf(nz - 1)};
+      xinv<3>(dp, specB_, d_.nx, ny, nz - 1, px_);
     }
-    DstFields<R, 1> d0{{F_[LESGO_P]}, 0, nz, d_.ld, kp_.plane};
-    xinv<1>(d0, specC_, 2 * pl_s, d_.nx, ny, 2, px_, "press.xinv_bc");
-    const long long n = (long long)d_.nx * ny * nz;
+    DstFields<R, 1> d0{{F_[LESGO_P]}, 0, nz, d_.ld, kp_.plane, imf(2)};
+    xinv<1>(d0, specC_, d_.nx, ny, 2, px_, "press.xinv_bc");
+    const long long n = (long long)d_.nx * ny * nz * kp_.ninst;
     pre();
     if (fused)
       k_wproj<R, true><<<grid1(n), 256, 0, st_>>>(F_[LESGO_P], F_[LESGO_DPDZ], F_[LESGO_RHSZ], F_[LESGO_U], F_[LESGO_V],
@@ -1142,7 +1332,7 @@ class Solver : public SolverBase {
 
   void turb_impl() {
     pre();
-    k_turb_disk<R><<<th_.n, 256, 0, st_>>>(td_, F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_.plane, d_.nz);
+    k_turb_disk<R><<<th_.n, 256, 0, st_>>>(td_, F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_.plane, d_.nz, kp_.istride);
     post("turbines.disk", (double)th_.node_q.size() * (4 * sizeof(R) + 16.0));
     if (td_.nwin > 0) {
       pre();
@@ -1156,10 +1346,13 @@ class Solver : public SolverBase {
   }
 
   Derived d_;
+  int cap_ = 1;
   KP kp_{};
   cudaStream_t st_ = nullptr;
   std::vector<void*> allocs_;
-  long long nfield_ = 0, vol_s_ = 0, vol_b_ = 0;
+  std::vector<Slot> slots_;
+  int next_id_ = 0;
+  long long nfield_ = 0, vol1_s_ = 0, vol1_b_ = 0;
   R* F_[LESGO_NFIELDS] = {};
   R* Ftmp_[4] = {};
   R* wall_[4] = {};
@@ -1169,6 +1362,8 @@ class Solver : public SolverBase {
   double2 *hspec_ = nullptr, *hplane_ = nullptr, *phat_ = nullptr;
   double* gam_ = nullptr;
   int* err_ = nullptr;
+  double* zo_d_ = nullptr;
+  int* flags_d_ = nullptr;
   double *diag_part_ = nullptr, *diag_out_ = nullptr;
   double* staging_ = nullptr;
   long long staging_n_ = 0;
@@ -1177,11 +1372,11 @@ class Solver : public SolverBase {
   double *kxw64_ = nullptr, *kyw64_ = nullptr;
   TurbineHost th_;
   TurbDev td_{};
+  IndicatorCache ind_cache_;
+  std::map<int, int> turb_base_;
   long long* cols_ = nullptr;
   double* tri_gam_ = nullptr;
   long long tri_gam_n_ = 0;
-  int jt_ = 0, jt_total_ = 0;
-  bool F_LM_MM_init_ = false, F_QN_NN_init_ = false;
   bool use_graphs_ = true, graphs_allowed_ = true;
   int launches_ = 0;
   bool prof_on_ = false;
@@ -1198,6 +1393,7 @@ class Solver : public SolverBase {
 // ---------------------------------------------------------------------------
 struct lesgo_handle {
   std::unique_ptr<lesgo::SolverBase> s;
+  int inst0 = -1;   // the instance of a single-instance handle (lesgo_gpu_create)
   std::string err;
   struct Bind { double* ptr = nullptr; int lbz = 0, nzhi = -1; };
   Bind bind[LESGO_NFIELDS];
@@ -1245,8 +1441,10 @@ int lesgo_gpu_create(const lesgo_params_t* p, lesgo_handle_t** h) {
     lesgo::Derived d(*p);
     auto* hh = new lesgo_handle;
     try {
-      if (p->precision == LESGO_FP64) hh->s.reset(new lesgo::Solver<double>(d));
-      else hh->s.reset(new lesgo::Solver<float>(d));
+      if (p->precision == LESGO_FP64) hh->s.reset(new lesgo::Solver<double>(d, 1));
+      else hh->s.reset(new lesgo::Solver<float>(d, 1));
+      lesgo::InstanceSpec spec{p->zo, 0, d.turbines};
+      hh->inst0 = hh->s->add_instance(spec);
     } catch (...) {
       delete hh;
       throw;
@@ -1286,11 +1484,11 @@ int lesgo_gpu_dims(const lesgo_handle_t* h, int* nz, int* ld, int* lh, int* nx2,
 
 int lesgo_gpu_set_field(lesgo_handle_t* h, int f, const double* host, int lbz, int nzhi) {
   if (!host) return LESGO_ERR_ARG;
-  return guarded(h, [&] { h->s->set_field(f, host, lbz, nzhi); });
+  return guarded(h, [&] { h->s->set_field(h->inst0, f, host, lbz, nzhi); });
 }
 int lesgo_gpu_get_field(lesgo_handle_t* h, int f, double* host, int lbz, int nzhi) {
   if (!host) return LESGO_ERR_ARG;
-  return guarded(h, [&] { h->s->get_field(f, host, lbz, nzhi); });
+  return guarded(h, [&] { h->s->get_field(h->inst0, f, host, lbz, nzhi); });
 }
 int lesgo_gpu_bind_field(lesgo_handle_t* h, int f, double* host, int lbz, int nzhi) {
   if (!h || !h->s || !host || f < 0 || f >= LESGO_NFIELDS) return LESGO_ERR_ARG;
@@ -1306,7 +1504,7 @@ int lesgo_gpu_download(lesgo_handle_t* h, int f) {
   if (!h || f < 0 || f >= LESGO_NFIELDS || !h->bind[f].ptr) return LESGO_ERR_ARG;
   return lesgo_gpu_get_field(h, f, h->bind[f].ptr, h->bind[f].lbz, h->bind[f].nzhi);
 }
-int lesgo_gpu_init_ic(lesgo_handle_t* h, uint64_t seed) { return guarded(h, [&] { h->s->init_ic(seed); }); }
+int lesgo_gpu_init_ic(lesgo_handle_t* h, uint64_t seed) { return guarded(h, [&] { h->s->init_ic(h->inst0, seed); }); }
 
 static bool fid_ok(int f) { return f >= 0 && f < LESGO_NFIELDS; }
 
@@ -1363,7 +1561,7 @@ int lesgo_gpu_sync(lesgo_handle_t* h) {
 }
 int lesgo_gpu_diag(lesgo_handle_t* h, double* rmsdiv, double* ke, double* cfl, double* tau_bot) {
   double out[4] = {0, 0, 0, 0};
-  int rc = guarded(h, [&] { h->s->diag(out); });
+  int rc = guarded(h, [&] { h->s->diag(h->inst0, out); });
   if (rc == LESGO_OK) {
     if (rmsdiv) *rmsdiv = out[0];
     if (ke) *ke = out[1];
@@ -1374,12 +1572,16 @@ int lesgo_gpu_diag(lesgo_handle_t* h, double* rmsdiv, double* ke, double* cfl, d
 }
 int lesgo_gpu_counters(const lesgo_handle_t* h, int* jt, int* jt_total) {
   if (!h || !h->s) return LESGO_ERR_ARG;
-  h->s->counters(jt, jt_total);
+  try {
+    h->s->counters(h->inst0, jt, jt_total);
+  } catch (...) {
+    return LESGO_ERR_ARG;
+  }
   return LESGO_OK;
 }
 int lesgo_gpu_turbine_state(lesgo_handle_t* h, double* u_d_T, double* f_n, double* power, int n) {
   if (n < 0) return LESGO_ERR_ARG;
-  return guarded(h, [&] { h->s->turbine_state(u_d_T, f_n, power, n); });
+  return guarded(h, [&] { h->s->turbine_state(h->inst0, u_d_T, f_n, power, n); });
 }
 int lesgo_gpu_launches_per_step(const lesgo_handle_t* h, int with_sgs_update) {
   if (!h || !h->s) return -1;
@@ -1496,3 +1698,90 @@ extern "C" int lesgo_gpu_tridag_array_noalloc(const double* a, const double* b, 
   if (flag) return noalloc_fail(LESGO_ERR_NUMERIC, "tridag_array_noalloc: zero pivot");
   return LESGO_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batches of independent instances of one grid size
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int lesgo_gpu_batch_create(const lesgo_params_t* p, int capacity, lesgo_handle_t** h) {
+  if (!p || !h || capacity < 1) return LESGO_ERR_ARG;
+  *h = nullptr;
+  try {
+    lesgo::Derived d(*p);
+    auto* hh = new lesgo_handle;
+    try {
+      if (p->precision == LESGO_FP64) hh->s.reset(new lesgo::Solver<double>(d, capacity));
+      else hh->s.reset(new lesgo::Solver<float>(d, capacity));
+    } catch (...) {
+      delete hh;
+      throw;
+    }
+    *h = hh;
+    return LESGO_OK;
+  } catch (const lesgo::Error& e) {
+    g_create_err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_create_err = e.what();
+    return LESGO_ERR_CUDA;
+  }
+}
+
+int lesgo_gpu_batch_add(lesgo_handle_t* h, double zo, uint64_t seed, int n_turbines, const lesgo_turbine_t* turbines,
+                        int* id) {
+  if (!id || n_turbines < 0 || (n_turbines > 0 && !turbines)) return LESGO_ERR_ARG;
+  return guarded(h, [&] {
+    lesgo::InstanceSpec spec{zo, seed, std::vector<lesgo_turbine_t>(turbines, turbines + n_turbines)};
+    *id = h->s->add_instance(spec);
+  });
+}
+
+int lesgo_gpu_batch_remove(lesgo_handle_t* h, int id) { return guarded(h, [&] { h->s->remove_instance(id); }); }
+
+int lesgo_gpu_batch_size(const lesgo_handle_t* h, int* active, int* capacity) {
+  if (!h || !h->s) return LESGO_ERR_ARG;
+  if (active) *active = h->s->active();
+  if (capacity) *capacity = h->s->capacity();
+  return LESGO_OK;
+}
+
+int lesgo_gpu_set_field_inst(lesgo_handle_t* h, int id, int f, const double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->set_field(id, f, host, lbz, nzhi); });
+}
+int lesgo_gpu_get_field_inst(lesgo_handle_t* h, int id, int f, double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->get_field(id, f, host, lbz, nzhi); });
+}
+int lesgo_gpu_diag_inst(lesgo_handle_t* h, int id, double* rmsdiv, double* ke, double* cfl, double* tau_bot) {
+  double out[4] = {0, 0, 0, 0};
+  int rc = guarded(h, [&] { h->s->diag(id, out); });
+  if (rc == LESGO_OK) {
+    if (rmsdiv) *rmsdiv = out[0];
+    if (ke) *ke = out[1];
+    if (cfl) *cfl = out[2];
+    if (tau_bot) *tau_bot = out[3];
+  }
+  return rc;
+}
+int lesgo_gpu_counters_inst(lesgo_handle_t* h, int id, int* jt, int* jt_total) {
+  return guarded(h, [&] { h->s->counters(id, jt, jt_total); });
+}
+int lesgo_gpu_turbine_state_inst(lesgo_handle_t* h, int id, double* u_d_T, double* f_n, double* power, int n) {
+  if (n < 0) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->turbine_state(id, u_d_T, f_n, power, n); });
+}
+int lesgo_gpu_footprint(const lesgo_params_t* p, int capacity, long long* bytes) {
+  if (!p || !bytes || capacity < 1) return LESGO_ERR_ARG;
+  try {
+    lesgo::Derived d(*p);
+    *bytes = lesgo::footprint_bytes(d, capacity);
+    return LESGO_OK;
+  } catch (const lesgo::Error& e) {
+    g_create_err = e.what();
+    return e.code;
+  }
+}
+
+}  // extern "C"

@@ -14,6 +14,23 @@ struct KP {
   double dt, tadv1, tadv2, vonk, zo, nu, delta, lagran_dt;
   double mpfx, mpfy, nu_nd, ubot, utop;
   int lbc, ubc, use_mpf, turbines;
+  int ninst;                 // instances (slots) stacked in every field
+  long long istride;         // elements between instances of a field: (nz+1)*plane
+  long long istride_big;     // same on the 3/2 grid
+  const double* zo_i;        // per-instance roughness length
+  const int* iflags;         // per-instance step flags (IF_*)
+};
+
+// Per-instance step flags: Euler first step (main.f90:273-280), Cs_opt2 =
+// 0.03 (sgs_stag_util.f90:187-189), dynamic update due this step
+// (:192-217), F_LM/F_MM and F_QN/F_NN initialisation (lagrange_Sdep.f90:266-276, 326-336).
+enum : int { IF_EULER = 1, IF_CSFILL = 2, IF_LAG = 4, IF_INITLM = 8, IF_INITQN = 16 };
+
+// Launch level index li -> (instance, level within the instance).
+struct InstMap {
+  int nli;          // levels per instance in this launch
+  long long istr;   // field elements between instances
+  __device__ __forceinline__ int inst(int li) const { return li / nli; }
 };
 
 // ---------------------------------------------------------------------------
@@ -26,8 +43,10 @@ struct SrcFields {
   R scale;
   int lev0, levstride, ld;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void load2(int n, int jy, int li, cplx<R>* v) const {
-    const long long off = (long long)(lev0 + li * levstride) * plane + (long long)jy * ld + 2 * n;
+    const int inst = im.inst(li), lv = li - inst * im.nli;
+    const long long off = inst * im.istr + (long long)(lev0 + lv * levstride) * plane + (long long)jy * ld + 2 * n;
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       cplx<R> a = *reinterpret_cast<const cplx<R>*>(p[f] + off);
@@ -44,9 +63,11 @@ struct SrcVort {
   R c;
   int ld, nz, lbc, ubc;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void load2(int n, int jy, int li, cplx<R>* out) const {
-    const int k = li + 1;
-    const long long o = (long long)k * plane + (long long)jy * ld + 2 * n;
+    const int inst = im.inst(li);
+    const int k = li - inst * im.nli + 1;
+    const long long o = inst * im.istr + (long long)k * plane + (long long)jy * ld + 2 * n;
     const long long om = o - plane, op = o + plane;
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
@@ -89,9 +110,11 @@ struct SrcConvProd {
   R c;
   int ld, nz;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void load2(int n, int jy, int li, cplx<R>* out) const {
-    const int k = li + 1;
-    const long long o = (long long)k * plane + (long long)jy * ld + 2 * n;
+    const int inst = im.inst(li);
+    const int k = li - inst * im.nli + 1;
+    const long long o = inst * im.istr + (long long)k * plane + (long long)jy * ld + 2 * n;
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       const long long q = o + e, qp = q + plane, qm = q - plane;
@@ -125,9 +148,11 @@ struct SrcLagrange {
   const R *u, *v, *w, *S11, *S12, *S13, *S22, *S23, *S33;
   int ld, nz, lbc, ubc;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void load2(int n, int jy, int li, cplx<R>* out) const {
-    const int k = li + 1;
-    const long long o = (long long)k * plane + (long long)jy * ld + 2 * n;
+    const int inst = im.inst(li);
+    const int k = li - inst * im.nli + 1;
+    const long long o = inst * im.istr + (long long)k * plane + (long long)jy * ld + 2 * n;
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       const long long q = o + e;
@@ -168,6 +193,7 @@ struct YOpLin {
   const InT* in;
   long long in_fs;       // elements between input fields (group g, input i -> g*NIN+i)
   int in_lev0, in_levstride, in_rows;
+  int nli, in_inst_levels;   // launch levels per instance; input planes per instance
   OutT* out;
   long long out_fs;
   int out_rows;
@@ -176,7 +202,9 @@ struct YOpLin {
   const R *kxw, *kyw, *G1, *G2;
 
   __device__ __forceinline__ cplx<R> load(int g, int i, int li, int jy, int kx) const {
-    const InT a = in[(long long)(g * NIN + i) * in_fs + ((long long)(in_lev0 + li * in_levstride) * in_rows + jy) * K + kx];
+    const int inst = li / nli, lv = li - inst * nli;
+    const long long plane_idx = (long long)inst * in_inst_levels + in_lev0 + lv * in_levstride;
+    const InT a = in[(long long)(g * NIN + i) * in_fs + (plane_idx * in_rows + jy) * K + kx];
     return mkc((R)a.x, (R)a.y);
   }
   __device__ __forceinline__ void store(int g, int o, int li, int ky, int kx, cplx<R> v) const {
@@ -217,8 +245,10 @@ struct DstFields {
   R* p[NF];
   int lev0, levstride, ld;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void store(int jy, int li, int i, const R* vals) const {
-    const long long off = (long long)(lev0 + li * levstride) * plane + (long long)jy * ld + i;
+    const int inst = im.inst(li), lv = li - inst * im.nli;
+    const long long off = inst * im.istr + (long long)(lev0 + lv * levstride) * plane + (long long)jy * ld + i;
 #pragma unroll
     for (int f = 0; f < NF; ++f) p[f][off] = vals[f];
   }
@@ -234,9 +264,11 @@ struct DstDiv {
   R inv_dz;
   int ld, nz;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void store(int jy, int li, int i, const R* vals) const {
-    const int k = li + 1;
-    const long long q = (long long)k * plane + (long long)jy * ld + i;
+    const int inst = im.inst(li);
+    const int k = li - inst * im.nli + 1;
+    const long long q = inst * im.istr + (long long)k * plane + (long long)jy * ld + i;
     int f = 0;
     if (WHICH & 1) {
       if (k <= nz - 1) {
@@ -261,17 +293,21 @@ struct DstConvec {
   R *RHSx, *RHSy, *RHSz, *RHSxf, *RHSyf, *RHSzf, *u, *v, *w;
   const R *divtx, *divty, *divtz, *fxa, *fya, *fza;
   double dt, t1, t2, mpfx, mpfy;
-  int ld, nz, euler, use_mpf, turbines;
+  int ld, nz, use_mpf, turbines;
+  const int* iflags;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void store(int jy, int li, int i, const R* vals) const {
-    const int k = li + 1;
-    const long long q = (long long)k * plane + (long long)jy * ld + i;
+    const int inst = im.inst(li);
+    const int k = li - inst * im.nli + 1;
+    const long long q = inst * im.istr + (long long)k * plane + (long long)jy * ld + i;
     if (!FUSED) {
       if (k <= nz - 1) { RHSx[q] = vals[0]; RHSy[q] = vals[1]; }
       RHSz[q] = vals[2];
       return;
     }
     const R dtr = (R)dt, t1r = (R)t1, t2r = (R)t2;
+    const bool euler = (iflags[inst] & IF_EULER) != 0;
     if (k <= nz - 1) {
       R nxr = -vals[0] - divtx[q];
       R nyr = -vals[1] - divty[q];
@@ -302,9 +338,11 @@ struct DstPress {
   double dt, t1;
   int ld;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void store(int jy, int li, int i, const R* vals) const {
-    const int k = li + 1;
-    const long long q = (long long)k * plane + (long long)jy * ld + i;
+    const int inst = im.inst(li);
+    const int k = li - inst * im.nli + 1;
+    const long long q = inst * im.istr + (long long)k * plane + (long long)jy * ld + i;
     p[q] = vals[0];
     if (!FUSED) {
       dpdx[q] = vals[1];
@@ -328,11 +366,17 @@ struct DstLagrange {
   const R *FLMi, *FMMi, *FQNi, *FNNi;  // interpolated running averages
   R *FLM, *FMM, *FQN, *FNN, *Cs, *Beta, *Tn_all, *ee_now;
   double cst, opftdelta, lagran_dt, beta_exp;
-  int ld, nz, lbc, ubc, init_lm, init_qn;
+  int ld, nz, lbc, ubc;
+  const int* iflags;
   long long plane;
+  InstMap im;
   __device__ __forceinline__ void store(int jy, int li, int i, const R* vals) const {
-    const int k = li + 1;
-    const long long q = (long long)k * plane + (long long)jy * ld + i;
+    const int inst = im.inst(li);
+    const int fl = iflags[inst];
+    if (!(fl & IF_LAG)) return;          // instance not due for the dynamic update
+    const bool init_lm = (fl & IF_INITLM) != 0, init_qn = (fl & IF_INITQN) != 0;
+    const int k = li - inst * im.nli + 1;
+    const long long q = inst * im.istr + (long long)k * plane + (long long)jy * ld + i;
     const R zero = (R)1.0e-24;
     const R tf1 = (R)2, tf2 = (R)4, tf1_2 = tf1 * tf1, tf2_2 = tf2 * tf2;
     auto A = [&](int qq) { return vals[2 * qq]; };

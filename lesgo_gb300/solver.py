@@ -37,35 +37,57 @@ PARAM_DEFAULTS = dict(
 )
 
 
+def make_params(**kw) -> L.Params:
+    """lesgo_params_t from lesgo.conf-style keywords (defaults: PARAM_DEFAULTS)."""
+    unknown = set(kw) - set(PARAM_DEFAULTS)
+    if unknown:
+        raise TypeError(f"unknown parameters: {sorted(unknown)}")
+    cfg = dict(PARAM_DEFAULTS, **kw)
+    p = L.Params()
+    p.nx, p.ny, p.nz_tot = cfg["nx"], cfg["ny"], cfg["Nz"]
+    for name in ("L_x", "L_y", "L_z", "z_i", "u_star", "vonk", "zo", "dt", "nu_molec", "ubot", "utop",
+                 "mean_p_force_x", "mean_p_force_y", "alpha1", "alpha2", "filter_cutoff", "T_avg_dim"):
+        setattr(p, name, float(cfg[name]))
+    for name in ("sgs_model", "cs_count", "dyn_init", "ifilter", "lbc_mom", "ubc_mom"):
+        setattr(p, name, int(cfg[name]))
+    for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction"):
+        setattr(p, name, 1 if cfg[name] else 0)
+    prec = cfg["precision"]
+    p.precision = {"fp64": L.LESGO_FP64, "mixed": L.LESGO_MIXED}[prec] if isinstance(prec, str) else int(prec)
+    return p, cfg
+
+
+def make_turbines(turbines):
+    tl = list(turbines or [])
+    arr = (L.Turbine * max(1, len(tl)))()
+    for i, t in enumerate(tl):
+        for k in ("xloc", "yloc", "height", "dia", "thk", "theta1", "theta2", "Ct_prime"):
+            setattr(arr[i], k, float(t.get(k, 1.33 if k == "Ct_prime" else 0.0)))
+    return arr, len(tl)
+
+
+def footprint_bytes(capacity: int = 1, **kw) -> int:
+    """Device bytes a handle of this grid and capacity allocates."""
+    lib = L.load()
+    p, _ = make_params(**kw)
+    b = C.c_longlong()
+    rc = lib.lesgo_gpu_footprint(C.byref(p), capacity, C.byref(b))
+    if rc != L.LESGO_OK:
+        raise LesgoError(rc, lib.lesgo_gpu_last_error(None).decode())
+    return b.value
+
+
 class LesgoGPU:
     """One LES instance resident on the current CUDA device."""
 
     def __init__(self, turbines: Optional[Iterable[dict]] = None, **kw):
-        unknown = set(kw) - set(PARAM_DEFAULTS)
-        if unknown:
-            raise TypeError(f"unknown parameters: {sorted(unknown)}")
-        cfg = dict(PARAM_DEFAULTS, **kw)
+        p, cfg = make_params(**kw)
         self.cfg = cfg
         self._lib = L.load()
-        p = L.Params()
-        p.nx, p.ny, p.nz_tot = cfg["nx"], cfg["ny"], cfg["Nz"]
-        for name in ("L_x", "L_y", "L_z", "z_i", "u_star", "vonk", "zo", "dt", "nu_molec", "ubot", "utop",
-                     "mean_p_force_x", "mean_p_force_y", "alpha1", "alpha2", "filter_cutoff", "T_avg_dim"):
-            setattr(p, name, float(cfg[name]))
-        for name in ("sgs_model", "cs_count", "dyn_init", "ifilter", "lbc_mom", "ubc_mom"):
-            setattr(p, name, int(cfg[name]))
-        for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction"):
-            setattr(p, name, 1 if cfg[name] else 0)
-        prec = cfg["precision"]
-        p.precision = {"fp64": L.LESGO_FP64, "mixed": L.LESGO_MIXED}[prec] if isinstance(prec, str) else int(prec)
-        tl = list(turbines or [])
-        self._turb = (L.Turbine * max(1, len(tl)))()
-        for i, t in enumerate(tl):
-            for k in ("xloc", "yloc", "height", "dia", "thk", "theta1", "theta2", "Ct_prime"):
-                setattr(self._turb[i], k, float(t.get(k, 0.0 if k.startswith("theta") else 1.33 if k == "Ct_prime" else 0.0)))
-        p.n_turbines = len(tl)
-        p.turbines = C.cast(self._turb, C.POINTER(L.Turbine)) if tl else None
-        self.n_turbines = len(tl)
+        self._turb, nt = make_turbines(turbines)
+        p.n_turbines = nt
+        p.turbines = C.cast(self._turb, C.POINTER(L.Turbine)) if nt else None
+        self.n_turbines = nt
         h = C.c_void_p()
         rc = self._lib.lesgo_gpu_create(C.byref(p), C.byref(h))
         if rc != L.LESGO_OK:
@@ -250,6 +272,112 @@ class LesgoGPU:
         s = C.c_void_p()
         self._check(self._lib.lesgo_gpu_get_stream(self._h, C.byref(s)))
         return s.value or 0
+
+    def launches_per_step(self, with_sgs_update: bool = False) -> int:
+        return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
+
+
+class LesgoBatch:
+    """A batch of independent LES instances of one grid size on the current
+    device.  All active instances advance together; each has its own
+    roughness length, IC seed, actuator disks and step counters."""
+
+    def __init__(self, capacity: int, **kw):
+        p, cfg = make_params(**kw)
+        self.cfg = cfg
+        self._lib = L.load()
+        h = C.c_void_p()
+        rc = self._lib.lesgo_gpu_batch_create(C.byref(p), capacity, C.byref(h))
+        if rc != L.LESGO_OK:
+            raise LesgoError(rc, self._lib.lesgo_gpu_last_error(None).decode())
+        self._h = h
+        nz, ld, lh, nx2, ny2 = (C.c_int() for _ in range(5))
+        self._lib.lesgo_gpu_dims(h, C.byref(nz), C.byref(ld), C.byref(lh), C.byref(nx2), C.byref(ny2))
+        self.nx, self.ny = cfg["nx"], cfg["ny"]
+        self.nz, self.ld = nz.value, ld.value
+        self.capacity = capacity
+        self._nturb = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lesgo_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != L.LESGO_OK:
+            raise LesgoError(rc, self._lib.lesgo_gpu_last_error(self._h).decode())
+
+    def add(self, zo: float, seed: int, turbines: Optional[Iterable[dict]] = None) -> int:
+        arr, nt = make_turbines(turbines)
+        i = C.c_int()
+        self._check(self._lib.lesgo_gpu_batch_add(self._h, float(zo), C.c_uint64(seed), nt,
+                                                  C.cast(arr, C.POINTER(L.Turbine)) if nt else None, C.byref(i)))
+        self._nturb[i.value] = nt
+        return i.value
+
+    def remove(self, iid: int):
+        self._check(self._lib.lesgo_gpu_batch_remove(self._h, iid))
+        self._nturb.pop(iid, None)
+
+    def size(self):
+        a, c = C.c_int(), C.c_int()
+        self._check(self._lib.lesgo_gpu_batch_size(self._h, C.byref(a), C.byref(c)))
+        return a.value, c.value
+
+    def get(self, iid: int, name, lbz: int = 0, nzhi: Optional[int] = None) -> np.ndarray:
+        nzhi = self.nz if nzhi is None else nzhi
+        out = np.empty((nzhi - lbz + 1, self.ny, self.ld), dtype=np.float64)
+        self._check(self._lib.lesgo_gpu_get_field_inst(self._h, iid, LesgoGPU._fid(name), out.ctypes.data, lbz, nzhi))
+        return out
+
+    def set(self, iid: int, name, arr: np.ndarray, lbz: int = 0):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self._check(self._lib.lesgo_gpu_set_field_inst(self._h, iid, LesgoGPU._fid(name), a.ctypes.data, lbz,
+                                                       lbz + a.shape[0] - 1))
+
+    def step(self, nsteps: int = 1):
+        self._check(self._lib.lesgo_gpu_step(self._h, nsteps))
+
+    def sync(self):
+        self._check(self._lib.lesgo_gpu_sync(self._h))
+
+    def diag(self, iid: int) -> Dict[str, float]:
+        r, k, c, t = (C.c_double() for _ in range(4))
+        self._check(self._lib.lesgo_gpu_diag_inst(self._h, iid, C.byref(r), C.byref(k), C.byref(c), C.byref(t)))
+        return dict(rmsdiv=r.value, ke=k.value, cfl=c.value, tau_bot=t.value)
+
+    def counters(self, iid: int):
+        a, b = C.c_int(), C.c_int()
+        self._check(self._lib.lesgo_gpu_counters_inst(self._h, iid, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def turbine_state(self, iid: int):
+        n = self._nturb.get(iid, 0)
+        a, b, c = (np.zeros(max(n, 1)) for _ in range(3))
+        dp = C.POINTER(C.c_double)
+        self._check(self._lib.lesgo_gpu_turbine_state_inst(self._h, iid, a.ctypes.data_as(dp), b.ctypes.data_as(dp),
+                                                           c.ctypes.data_as(dp), n))
+        return dict(u_d_T=a[:n], f_n=b[:n], power=c[:n])
+
+    def stream_ptr(self) -> int:
+        s = C.c_void_p()
+        self._check(self._lib.lesgo_gpu_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def profile(self, enable: bool = True):
+        self._check(self._lib.lesgo_gpu_profile(self._h, 1 if enable else 0))
+
+    def profile_report(self) -> dict:
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        self._check(self._lib.lesgo_gpu_profile_report(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
 
     def launches_per_step(self, with_sgs_update: bool = False) -> int:
         return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)

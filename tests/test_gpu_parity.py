@@ -168,3 +168,31 @@ def test_turbines_fp64(built_lib):
     for f in ("u", "w"):
         e = rel_err(p, f, g2.get(f), g.get(f))
         assert e < 1e-11, (f, e)
+
+
+def test_batch_alone_equals_mixed(built_lib):
+    """Each instance of a batch (own roughness and seed, one with actuator
+    disks) equals the same instance run alone: fields identical bit for bit
+    in FP64 and in the mixed form, including an instance admitted late and
+    after a removal compacted the batch."""
+    from lesgo_gb300.solver import LesgoBatch, LesgoGPU
+    ts, _ = _farm(1, 2)
+    base = dict(nx=32, ny=32, Nz=24, dyn_init=3, cs_count=3)
+    specs = [(1e-4, 11, None), (3e-5, 12, ts), (8e-4, 13, None)]
+    for prec in ("fp64", "mixed"):
+        b = LesgoBatch(capacity=4, precision=prec, **base)
+        ids = [b.add(zo, seed, tb) for zo, seed, tb in specs]
+        b.step(4)
+        b.remove(ids[0])                         # compaction moves the last instance
+        late = b.add(2e-4, 14)                   # admitted later, its own step count
+        b.step(5)
+        for (zo, seed, tb), iid, nsteps in [(specs[1], ids[1], 9), (specs[2], ids[2], 9), ((2e-4, 14, None), late, 5)]:
+            g = LesgoGPU(turbines=tb, zo=zo, precision=prec, **base)
+            g.init_ic(seed)
+            g.step(nsteps)
+            for f in ("u", "v", "w", "p", "Cs_opt2", "F_LM"):
+                a, c = b.get(iid, f), g.get(f)
+                assert np.array_equal(a[1:g.nz], c[1:g.nz]), (prec, iid, f, np.max(np.abs(a - c)))
+            assert b.counters(iid) == g.counters()
+            g.close()
+        b.close()
