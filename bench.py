@@ -49,7 +49,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--forms", default="fp64,mixed")
+    ap.add_argument("--forms", default="fp64,mixed,batched")
+    ap.add_argument("--serve", action="store_true", help="run the served request stream instead")
+    ap.add_argument("--requests", type=int, default=24)
     return ap.parse_args()
 
 
@@ -157,6 +159,75 @@ def time_form(precision, args, torch, world):
     return dict(ms=ms, steps=steps, pts=n * n * n, launches=launches, profile=rep, diag=diag, cfg=cfg)
 
 
+BATCH_GRIDS = [(48, 48, 48), (64, 64, 64), (96, 96, 64), (128, 64, 64)]
+
+
+def batch_instances(n=48, seed=2024):
+    """The 48-instance ensemble: grid drawn from BATCH_GRIDS, z0 log-uniform
+    in [1e-5, 1e-3], own IC seed."""
+    import math
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        g = BATCH_GRIDS[int(rng.integers(len(BATCH_GRIDS)))]
+        zo = math.exp(rng.uniform(math.log(1e-5), math.log(1e-3)))
+        out.append((g, zo, 5000 + i))
+    return out
+
+
+def time_batched(args, torch):
+    """All 48 instances in the mixed form: one batch handle per grid size
+    (every kernel advances the whole class in one launch), classes on their
+    own streams and overlapping; against the same instances run one at a
+    time in the plain FP64 form."""
+    from lesgo_gb300.solver import LesgoBatch, LesgoGPU
+    inst = batch_instances()
+    by_grid = {}
+    for g, zo, seed in inst:
+        by_grid.setdefault(g, []).append((zo, seed))
+    batches = []
+    for g, lst in by_grid.items():
+        b = LesgoBatch(len(lst), nx=g[0], ny=g[1], Nz=g[2], precision="mixed", dyn_init=5, cs_count=5)
+        for zo, seed in lst:
+            b.add(zo, seed)
+        batches.append((g, len(lst), b))
+    for _, _, b in batches:
+        b.step(10)
+    for _, _, b in batches:
+        b.sync()
+    steps = max(5, (args.steps + 4) // 5 * 5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for _, _, b in batches:
+            b.step(1)
+    for _, _, b in batches:
+        b.sync()
+    dt = time.perf_counter() - t0
+    pts = sum(g[0] * g[1] * g[2] * n for g, n, _ in batches)
+    launches = sum((4 * b.launches_per_step(False) + b.launches_per_step(True)) for _, _, b in batches) * steps // 5
+    for _, _, b in batches:
+        b.close()
+    # plain FP64, one instance at a time: steady-state step time per grid
+    t64 = {}
+    for g in by_grid:
+        s = LesgoGPU(nx=g[0], ny=g[1], Nz=g[2], precision="fp64", dyn_init=5, cs_count=5)
+        s.init_ic(1)
+        s.step(10)
+        s.sync()
+        t1 = time.perf_counter()
+        s.step(10)
+        s.sync()
+        t64[g] = (time.perf_counter() - t1) / 10
+        s.close()
+    seq_time = sum(t64[g] for g, _, _ in inst)
+    fp64_one_at_a_time = sum(g[0] * g[1] * g[2] for g, _, _ in inst) / seq_time
+    return dict(value=pts * steps / dt, ms_per_step=dt * 1e3 / steps, instances=len(inst),
+                grids={f"{g[0]}x{g[1]}x{g[2]}": n for g, n, _ in batches}, launches=launches,
+                fp64_one_at_a_time=fp64_one_at_a_time, ratio_vs_fp64_one_at_a_time=pts * steps / dt / fp64_one_at_a_time)
+
+
 def time_e2e(args, torch):
     """Through the C ABI with host buffers: per step, u, v, w go host->device
     from pinned memory, one fused step runs, and u, v, w come back."""
@@ -225,7 +296,7 @@ def run_ours(args):
     hbm, peak_kind = peaks()
     forms = [f for f in args.forms.split(",") if f]
     with Clocks(local) as clk:
-        res = {f: time_form(f, args, torch, world) for f in forms}
+        res = {f: time_form(f, args, torch, world) for f in forms if f in ("fp64", "mixed")}
     clocks = clk.summary()
     head = res.get("fp64") or next(iter(res.values()))
     ms = head["ms"]
@@ -234,6 +305,7 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = head["pts"] * head["steps"] * world / (ms * 1e-3)
+    batched = time_batched(args, torch) if "batched" in forms else None
     e2e = time_e2e(args, torch) if rank == 0 else None
     cpu = cpu_baseline(args) if (rank == 0 and world == 1 and not args.no_cpu) else None
     if rank != 0:
@@ -252,6 +324,8 @@ def run_ours(args):
                             dominant_frac=rf["frac"], dominant_share=rf["share"], diag=r["diag"])
     if "fp64" in out_forms and "mixed" in out_forms:
         out_forms["mixed_vs_fp64"] = out_forms["mixed"]["value"] / out_forms["fp64"]["value"]
+    if batched:
+        out_forms["mixed_batched"] = batched
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": head["steps"],
         "warmup": args.warmup, "ms_per_step": ms / head["steps"], "higher_is_better": True, "scaling": "weak",
@@ -316,10 +390,50 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Served stream: Poisson arrivals; grid from {64^3, 128x128x96,
+    192x192x128}; z0 log-uniform in [1e-5, 1e-3]; 0-16 actuator disks;
+    200-2000 steps; 150 GB admission budget; mixed form.  Reports p50/p99
+    completion latency and aggregate grid-point-steps/s next to the plain FP64
+    form run one request at a time (from measured steady-state step times)."""
+    import torch
+    torch.cuda.set_device(0)
+    from lesgo_gb300.serve import GpuBackend, Server, poisson_requests
+    from lesgo_gb300.solver import LesgoGPU
+    grids = [(64, 64, 64), (128, 128, 96), (192, 192, 128)]
+    base = dict(dyn_init=100, cs_count=5)
+    # arrival rate sized to keep the GPU busy: mean work / mean service time
+    reqs = poisson_requests(args.requests, rate=4.0, grids=grids, steps_range=(200, 2000), seed=7, turbines_max=16)
+    srv = Server(GpuBackend("mixed", **base), budget_bytes=150e9, chunk_slots=8, cs_count=5)
+    rep = srv.run(reqs)
+    t64 = {}
+    for g in grids:
+        s = LesgoGPU(nx=g[0], ny=g[1], Nz=g[2], precision="fp64", **base)
+        s.init_ic(1)
+        s.step(5)
+        s.sync()
+        t1 = time.perf_counter()
+        s.step(10)
+        s.sync()
+        t64[g] = (time.perf_counter() - t1) / 10
+        s.close()
+    seq = sum(r.steps * t64[r.grid] for r in reqs)
+    one_at_a_time = sum(r.points * r.steps for r in reqs) / seq
+    line = {"metric": "served LES requests: aggregate grid-pt-steps/s and completion latency", "unit": UNIT,
+            "value": rep["throughput"], "p50_s": rep["p50_s"], "p99_s": rep["p99_s"], "requests": rep["requests"],
+            "wall_s": rep["wall_s"], "busy_frac": rep["busy_frac"], "fp64_one_at_a_time": one_at_a_time,
+            "ratio_vs_fp64_one_at_a_time": rep["throughput"] / one_at_a_time, "budget_gb": 150,
+            "config": {"grids": [list(g) for g in grids], "steps": [200, 2000], "turbines": [0, 16],
+                       "arrival_rate_per_s": 4.0, "form": "mixed (FP32 bulk, FP64 pressure solve)"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.serve:
+        run_serve(args)
     else:
         run_ours(args)
 
