@@ -321,7 +321,8 @@ def run_ours(args):
         v = r["pts"] * r["steps"] * world / (r["ms"] * 1e-3)
         kn, rf = dominant(r["profile"], hbm)
         out_forms[f] = dict(value=v, ms_per_step=r["ms"] / r["steps"], dominant_kernel=kn,
-                            dominant_frac=rf["frac"], dominant_share=rf["share"], diag=r["diag"])
+                            dominant_frac=rf["frac"], dominant_share=rf["share"], diag=r["diag"],
+                            kernels=r["profile"])
     if "fp64" in out_forms and "mixed" in out_forms:
         out_forms["mixed_vs_fp64"] = out_forms["mixed"]["value"] / out_forms["fp64"]["value"]
     if batched:

@@ -330,11 +330,16 @@ __global__ void k_interp(InterpArgs<R> a) {
     yq = y - 0.5 * ((double)a.v[q - P] + (double)a.v[q]) * ldt;
     zq = zwc(k) - (double)a.w[q] * ldt;
   }
+  // cell_indx_w with reciprocal multiplies (FP64 division is a long DFMA
+  // sequence on this part); the weights differ from the reference's
+  // divisions by at most an ulp, and a cell flip at an exact face leaves the
+  // linear interpolant unchanged
   const double thresh = 1.0e-9;
-  double px = fmodulo(xq, kp.L_x);
-  int ist = (fabs(px) / kp.L_x < thresh) ? 1 : (fabs(px - kp.L_x) / kp.L_x < thresh) ? kp.nx : (int)floor(px / kp.dx) + 1;
-  double py = fmodulo(yq, kp.L_y);
-  int jst = (fabs(py) / kp.L_y < thresh) ? 1 : (fabs(py - kp.L_y) / kp.L_y < thresh) ? kp.ny : (int)floor(py / kp.dy) + 1;
+  const double idx = 1.0 / kp.dx, idy = 1.0 / kp.dy, idz = 1.0 / dz;
+  double px = xq - floor(xq * (1.0 / kp.L_x)) * kp.L_x;
+  int ist = (fabs(px) < thresh * kp.L_x) ? 1 : (fabs(px - kp.L_x) < thresh * kp.L_x) ? kp.nx : (int)floor(px * idx) + 1;
+  double py = yq - floor(yq * (1.0 / kp.L_y)) * kp.L_y;
+  int jst = (fabs(py) < thresh * kp.L_y) ? 1 : (fabs(py - kp.L_y) < thresh * kp.L_y) ? kp.ny : (int)floor(py * idy) + 1;
   ist = min(max(ist, 1), kp.nx);
   jst = min(max(jst, 1), kp.ny);
   const int ist1 = ist + 1 > kp.nx ? 1 : ist + 1;
@@ -350,31 +355,32 @@ __global__ void k_interp(InterpArgs<R> a) {
     if (zq > zc(nz - 1)) { kst = nz; kst1 = nz; zdiff = 0.0; }
     else { kst = nz - 1; kst1 = nz; zdiff = 2.0 * (zq - zwc(nz - 1)); }
   } else {
-    if (fabs(zq - zwc(nz)) / kp.L_z < thresh) kst = nz - 1;
-    else kst = (int)floor((zq - zwc(1)) / dz) + 1;
+    if (fabs(zq - zwc(nz)) < thresh * kp.L_z) kst = nz - 1;
+    else kst = (int)floor((zq - zwc(1)) * idz) + 1;
     // the reference assumes a Lagrangian CFL below one, which keeps kst in
     // 1..nz-1; the clamp only guards the memory access
     kst = min(max(kst, 1), nz - 1);
     kst1 = kst + 1;
     zdiff = zq - zwc(kst);
   }
+  const R wx = (R)(xdiff * idx), wy = (R)(ydiff * idy), wz = (R)(zdiff * idz);
   const long long b00 = ib + (long long)(jst - 1) * kp.ld, b01 = ib + (long long)(jst1 - 1) * kp.ld;
   const int i0 = ist - 1, i1 = ist1 - 1;
   const long long z0 = kst * P, z1 = kst1 * P;
 #pragma unroll
   for (int f = 0; f < 4; ++f) {
     const R* V = a.Fin[f];
-    const double v000 = V[z0 + b00 + i0], v001 = V[z0 + b00 + i1];
-    const double v010 = V[z0 + b01 + i0], v011 = V[z0 + b01 + i1];
-    const double v100 = V[z1 + b00 + i0], v101 = V[z1 + b00 + i1];
-    const double v110 = V[z1 + b01 + i0], v111 = V[z1 + b01 + i1];
-    const double u1 = v000 + xdiff * (v001 - v000) / kp.dx;
-    const double u2 = v010 + xdiff * (v011 - v010) / kp.dx;
-    const double u3 = v100 + xdiff * (v101 - v100) / kp.dx;
-    const double u4 = v110 + xdiff * (v111 - v110) / kp.dx;
-    const double u5 = u1 + ydiff * (u2 - u1) / kp.dy;
-    const double u6 = u3 + ydiff * (u4 - u3) / kp.dy;
-    a.Fout[f][q] = (R)(u5 + zdiff * (u6 - u5) / dz);
+    const R v000 = V[z0 + b00 + i0], v001 = V[z0 + b00 + i1];
+    const R v010 = V[z0 + b01 + i0], v011 = V[z0 + b01 + i1];
+    const R v100 = V[z1 + b00 + i0], v101 = V[z1 + b00 + i1];
+    const R v110 = V[z1 + b01 + i0], v111 = V[z1 + b01 + i1];
+    const R u1 = v000 + wx * (v001 - v000);
+    const R u2 = v010 + wx * (v011 - v010);
+    const R u3 = v100 + wx * (v101 - v100);
+    const R u4 = v110 + wx * (v111 - v110);
+    const R u5 = u1 + wy * (u2 - u1);
+    const R u6 = u3 + wy * (u4 - u3);
+    a.Fout[f][q] = u5 + wz * (u6 - u5);
   }
 }
 
