@@ -45,12 +45,36 @@ template <typename T2> __device__ __forceinline__ T2 mul_pi(T2 a) { return mkc(-
 
 constexpr int kMaxStages = 12;
 
+// Unsigned division by a run-time constant d >= 1 for dividends below 2^31,
+// with one multiply-high and a shift: l = ceil(log2 d), p = 31 + l,
+// m = ceil(2^p / d), q = umulhi(n, m) >> (l - 1) (Granlund and Montgomery's
+// round-up reciprocal; the error m*d - 2^p < d keeps the quotient exact for
+// n < 2^31).  Integer division would otherwise be a long instruction
+// sequence inside every butterfly and every element copy.
+struct FastDiv {
+  unsigned d = 1, m = 0, sh = 0;
+  FastDiv() = default;
+  __host__ explicit FastDiv(unsigned dv) : d(dv) {
+    if (dv <= 1) { d = 1; return; }
+    unsigned l = 0;
+    while ((1u << l) < dv) ++l;
+    m = (unsigned)(((1ull << (31 + l)) + dv - 1) / dv);
+    sh = l - 1;
+  }
+  __device__ __forceinline__ int div(int n) const {
+    return d == 1 ? n : (int)(__umulhi((unsigned)n, m) >> sh);
+  }
+};
+
 // Plan for one complex FFT length n = prod(radix[]).
 template <typename R>
 struct FftPlan {
   int n;
   int nf;
   int radix[kMaxStages];
+  int nbs[kMaxStages];        // butterflies per line in stage s (n / radix[s])
+  int nss[kMaxStages];        // sub-transform length Ns entering stage s
+  FastDiv fnb[kMaxStages], fns[kMaxStages];
   const cplx<R>* tw;   // tw[t] = exp(-2 pi i t / n), t = 0..n-1
   const cplx<R>* rtw;  // rtw[k] = exp(-2 pi i k / (2n)), k = 0..n (real-transform packing)
 };
@@ -129,19 +153,20 @@ __device__ __forceinline__ T2 twid(const T2* tw, int idx, T2 a) {
 template <typename R, bool INV>
 __device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FftPlan<R>& p) {
   using T2 = cplx<R>;
-  const int n = p.n;
-  int Ns = 1;
   for (int s = 0; s < p.nf; ++s) {
     const int Rr = p.radix[s];
-    const int nb = n / Rr;
+    const int nb = p.nbs[s];
+    const int Ns = p.nss[s];
     const int total = nl * nb;
-    const int tws = n / (Ns * Rr);
+    const int tws = nb / Ns;            // n / (Ns * Rr)
+    const FastDiv fnb = p.fnb[s], fns = p.fns[s];
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int l = t / nb;
+      const int l = fnb.div(t);
       const int j = t - l * nb;
-      const int jm = j % Ns;
+      const int q = fns.div(j);
+      const int jm = j - q * Ns;
       const T2* src = a + l * ls + j;
-      T2* dst = b + l * ls + (j - jm) * Rr + jm;
+      T2* dst = b + l * ls + q * Ns * Rr + jm;
       const int tb = jm * tws;
       if (Rr == 4) {
         T2 v0 = src[0], v1 = src[nb], v2 = src[2 * nb], v3 = src[3 * nb];
@@ -180,7 +205,6 @@ __device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FftP
     }
     __syncthreads();
     cplx<R>* tmp = a; a = b; b = tmp;
-    Ns *= Rr;
   }
   return a;
 }
@@ -196,6 +220,7 @@ struct XfGeom {
   int rpc;      // rows per CTA
   int ls;       // smem line stride (complex)
   long long out_field_stride;  // complex elements between fields in the output
+  FastDiv fH, fK, fnyrows, frpc;   // by M/2, K, nyrows, rpc
 };
 
 // Xf: r2c along x for NF fields at once.  Src::load2(n, jy, li, v[NF])
@@ -211,11 +236,11 @@ __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src
   const int H = g.M / 2;
   const int row0 = blockIdx.x * g.rpc;
   for (int t = threadIdx.x; t < g.rpc * H; t += blockDim.x) {
-    const int r = t / H, nn = t - r * H;
+    const int r = g.fH.div(t), nn = t - r * H;
     const int row = row0 + r;
     T2 v[NF];
     if (row < g.nrows) {
-      const int li = row / g.nyrows;
+      const int li = g.fnyrows.div(row);
       const int jy = row - li * g.nyrows;
       src.load2(nn, jy, li, v);
     } else {
@@ -229,8 +254,8 @@ __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src
   T2* Z = fft_lines<R, false>(A, B, nl, g.ls, plan);
   const R half = (R)0.5;
   for (int t = threadIdx.x; t < nl * g.K; t += blockDim.x) {
-    const int l = t / g.K, kk = t - l * g.K;
-    const int f = l / g.rpc, r = l - f * g.rpc;
+    const int l = g.fK.div(t), kk = t - l * g.K;
+    const int f = g.frpc.div(l), r = l - f * g.rpc;
     const int row = row0 + r;
     if (row >= g.nrows) continue;
     T2 zk = Z[l * g.ls + kk];
@@ -252,6 +277,7 @@ struct XiGeom {
   int rpc;
   int ls;
   long long in_field_stride;
+  FastDiv fH, fM, fnyrows, frpc;   // by M/2, M, nyrows, rpc
 };
 
 // Xi: c2r along x for NF fields at once, then Dst::store(jy, li, i, vals)
@@ -267,8 +293,8 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
   const int row0 = blockIdx.x * g.rpc;
   // build Z[k] = (X[k] + conj X[H-k]) + i W^-k (X[k] - conj X[H-k])
   for (int t = threadIdx.x; t < nl * H; t += blockDim.x) {
-    const int l = t / H, k = t - l * H;
-    const int f = l / g.rpc, r = l - f * g.rpc;
+    const int l = g.fH.div(t), k = t - l * H;
+    const int f = g.frpc.div(l), r = l - f * g.rpc;
     const int row = row0 + r;
     T2 z = mkc((R)0, (R)0);
     if (row < g.nrows) {
@@ -288,10 +314,10 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
   T2* Z = fft_lines<R, true>(A, B, nl, g.ls, plan);
   const R* Zr = reinterpret_cast<const R*>(Z);
   for (int t = threadIdx.x; t < g.rpc * g.M; t += blockDim.x) {
-    const int r = t / g.M, i = t - r * g.M;
+    const int r = g.fM.div(t), i = t - r * g.M;
     const int row = row0 + r;
     if (row >= g.nrows) continue;
-    const int li = row / g.nyrows;
+    const int li = g.fnyrows.div(row);
     const int jy = row - li * g.nyrows;
     R vals[NF];
 #pragma unroll
@@ -308,6 +334,8 @@ struct YGeom {
   int ls_in, ls_out;
   long long in_lev_stride;   // complex elements between planes of the input
   long long out_lev_stride;
+  int tk_log2;               // tk is a power of two
+  FastDiv fny_in, fny_out;
 };
 
 // Y pass.  NIN input spectra (after Xf) are loaded per column tile and, if
@@ -331,10 +359,10 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
   const int tk = min(g.tk, g.K - kx0);
   // load inputs: element (jy, c) of input i
   for (int t = threadIdx.x; t < NIN * g.ny_in * g.tk; t += blockDim.x) {
-    const int c = t % g.tk;
-    const int rest = t / g.tk;
-    const int jy = rest % g.ny_in;
-    const int i = rest / g.ny_in;
+    const int c = t & (g.tk - 1);
+    const int rest = t >> g.tk_log2;
+    const int i = g.fny_in.div(rest);
+    const int jy = rest - i * g.ny_in;
     T2 v = mkc((R)0, (R)0);
     if (c < tk) v = op.load(grp, i, li, jy, kx0 + c);
     S[(i * g.tk + c) * g.ls_in + jy] = v;
@@ -349,7 +377,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
   }
   for (int o = 0; o < NOUT; ++o) {
     for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
-      const int c = t / g.ny_out, ky = t - c * g.ny_out;
+      const int c = g.fny_out.div(t), ky = t - c * g.ny_out;
       const int kx = kx0 + c;
       T2 acc = mkc((R)0, (R)0);
       const int kin = op.rowmap(ky);
@@ -369,7 +397,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
     T2* res = W0;
     if (INV) res = fft_lines<R, true>(W0, W1, g.tk, g.ls_out, pout);
     for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
-      const int ky = t / g.tk, c = t - ky * g.tk;
+      const int ky = t >> g.tk_log2, c = t & (g.tk - 1);
       if (c < tk) op.store(grp, o, li, ky, kx0 + c, res[c * g.ls_out + ky]);
     }
     __syncthreads();

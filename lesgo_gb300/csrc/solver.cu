@@ -825,7 +825,7 @@ class Solver : public SolverBase {
   void need_active() const {
     if (slots_.empty()) throw Error(LESGO_ERR_ARG, "no active instance");
   }
-  InstMap imf(int nli) const { return InstMap{nli, kp_.istride}; }
+  InstMap imf(int nli) const { return InstMap(nli, kp_.istride); }
 
   void sync_instance_params() {
     kp_.ninst = (int)slots_.size();
@@ -1010,7 +1010,15 @@ class Solver : public SolverBase {
     p.n = n;
     auto r = factorize(n);
     p.nf = (int)r.size();
-    for (int i = 0; i < p.nf; ++i) p.radix[i] = r[i];
+    int ns = 1;
+    for (int i = 0; i < p.nf; ++i) {
+      p.radix[i] = r[i];
+      p.nbs[i] = n / r[i];
+      p.nss[i] = ns;
+      p.fnb[i] = FastDiv((unsigned)p.nbs[i]);
+      p.fns[i] = FastDiv((unsigned)ns);
+      ns *= r[i];
+    }
     std::vector<T2> tw(n), rtw(n + 1);
     for (int t = 0; t < n; ++t) {
       const long double a = -2.0L * kPiL * (long double)t / (long double)n;
@@ -1095,6 +1103,8 @@ class Solver : public SolverBase {
     const int target = sizeof(R) == 8 ? 2048 : 4096;
     g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
     g.out_field_stride = (long long)g.nrows * g.K;
+    g.fH = FastDiv((unsigned)(M / 2)); g.fK = FastDiv((unsigned)g.K);
+    g.fnyrows = FastDiv((unsigned)nyrows); g.frpc = FastDiv((unsigned)g.rpc);
     const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
     auto kern = k_xfwd<R, NF, Src>;
     set_smem(kern, smem);
@@ -1111,6 +1121,8 @@ class Solver : public SolverBase {
     const int target = sizeof(R) == 8 ? 2048 : 4096;
     g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
     g.in_field_stride = (long long)g.nrows * g.K;
+    g.fH = FastDiv((unsigned)(M / 2)); g.fM = FastDiv((unsigned)M);
+    g.fnyrows = FastDiv((unsigned)nyrows); g.frpc = FastDiv((unsigned)g.rpc);
     const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
     auto kern = k_xinv<R, NF, Dst>;
     set_smem(kern, smem);
@@ -1131,7 +1143,7 @@ class Solver : public SolverBase {
     op.in = in;
     op.in_fs = (long long)in_inst_levels * kp_.ninst * in_rows * d_.K;
     op.in_lev0 = in_lev0; op.in_levstride = in_levstride; op.in_rows = in_rows;
-    op.nli = nli; op.in_inst_levels = in_inst_levels;
+    op.nli = nli; op.in_inst_levels = in_inst_levels; op.fnli = FastDiv((unsigned)nli);
     op.out = out; op.out_fs = (long long)nlev * out_rows * d_.K; op.out_rows = out_rows;
     op.K = d_.K; op.lh = d_.lh; op.ny_small = d_.ny; op.ny_big = d_.ny2; op.rowmode = rowmode;
     int o = 0;
@@ -1154,8 +1166,11 @@ class Solver : public SolverBase {
       return (s + std::max(s, (size_t)2 * t * g.ls_out)) * sizeof(T2);
     };
     while (tk > 1 && smem_of(tk) > budget) tk /= 2;
-    tk = std::min(tk, d_.K);
+    while (tk > d_.K) tk /= 2;          // tk stays a power of two
     g.tk = tk;
+    g.tk_log2 = 0;
+    while ((1 << g.tk_log2) < tk) ++g.tk_log2;
+    g.fny_in = FastDiv((unsigned)in_rows); g.fny_out = FastDiv((unsigned)out_rows);
     g.in_lev_stride = 0; g.out_lev_stride = 0;
     const size_t smem = smem_of(tk);
     auto kern = k_ypass<R, NIN, NOUT, FWD, INV, YOpLin<R, NIN, NOUT, InT, OutT>>;
@@ -1177,10 +1192,10 @@ class Solver : public SolverBase {
     xfwd<2>(src, d_.nx, d_.ny, 1, in, px_, "wall_filter.xfwd");
     ypass_lin<1, 1, true, true, T2, T2>(in, 0, 1, 1, d_.ny, outp, d_.ny, 1, 2, ROW_SAME, {{MUL_G1}}, "wall_filter.ypass");
     if (nf == 1) {
-      DstFields<R, 1> dst{{oa}, 0, 1, d_.ld, 0, InstMap{1, ostr}};
+      DstFields<R, 1> dst{{oa}, 0, 1, d_.ld, 0, InstMap(1, ostr)};
       xinv<1>(dst, outp, d_.nx, d_.ny, 1, px_, "wall_filter.xinv");
     } else {
-      DstFields<R, 2> dst{{oa, ob}, 0, 1, d_.ld, 0, InstMap{1, ostr}};
+      DstFields<R, 2> dst{{oa, ob}, 0, 1, d_.ld, 0, InstMap(1, ostr)};
       xinv<2>(dst, outp, d_.nx, d_.ny, 1, px_, "wall_filter.xinv");
     }
   }
@@ -1248,7 +1263,7 @@ class Solver : public SolverBase {
   void convec_impl(bool fused) {
     const R c = (R)(1.0 / ((double)d_.nx * d_.ny));
     const InstMap im = imf(d_.nz);
-    const InstMap imb{d_.nz, kp_.istride_big};
+    const InstMap imb(d_.nz, kp_.istride_big);
     SrcVort<R> sv{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDY], F_[LESGO_DUDZ], F_[LESGO_DVDX],
                   F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane, im};
     xfwd<6>(sv, d_.nx, d_.ny, d_.nz, specA_, px_, "convec.xfwd", 9);

@@ -28,9 +28,12 @@ enum : int { IF_EULER = 1, IF_CSFILL = 2, IF_LAG = 4, IF_INITLM = 8, IF_INITQN =
 
 // Launch level index li -> (instance, level within the instance).
 struct InstMap {
-  int nli;          // levels per instance in this launch
-  long long istr;   // field elements between instances
-  __device__ __forceinline__ int inst(int li) const { return li / nli; }
+  int nli = 1;          // levels per instance in this launch
+  long long istr = 0;   // field elements between instances
+  FastDiv fd;
+  InstMap() = default;
+  __host__ InstMap(int n, long long s) : nli(n), istr(s), fd((unsigned)n) {}
+  __device__ __forceinline__ int inst(int li) const { return fd.div(li); }
 };
 
 // ---------------------------------------------------------------------------
@@ -194,6 +197,7 @@ struct YOpLin {
   long long in_fs;       // elements between input fields (group g, input i -> g*NIN+i)
   int in_lev0, in_levstride, in_rows;
   int nli, in_inst_levels;   // launch levels per instance; input planes per instance
+  FastDiv fnli;
   OutT* out;
   long long out_fs;
   int out_rows;
@@ -202,7 +206,7 @@ struct YOpLin {
   const R *kxw, *kyw, *G1, *G2;
 
   __device__ __forceinline__ cplx<R> load(int g, int i, int li, int jy, int kx) const {
-    const int inst = li / nli, lv = li - inst * nli;
+    const int inst = fnli.div(li), lv = li - inst * nli;
     const long long plane_idx = (long long)inst * in_inst_levels + in_lev0 + lv * in_levstride;
     const InT a = in[(long long)(g * NIN + i) * in_fs + (plane_idx * in_rows + jy) * K + kx];
     return mkc((R)a.x, (R)a.y);
