@@ -298,8 +298,6 @@ struct InterpArgs {
   KP kp;
 };
 
-__device__ __forceinline__ double fmodulo(double a, double p) { return a - floor(a / p) * p; }
-
 template <typename R>
 __global__ void k_interp(InterpArgs<R> a) {
   const KP& kp = a.kp;
@@ -385,95 +383,153 @@ __global__ void k_interp(InterpArgs<R> a) {
 }
 
 // ---------------------------------------------------------------------------
-// press_stag_array.f90:186-234 + tridag_array.f90:166-246: one Thomas solve
-// per (kx, ky) column in FP64, the kx = ky = 0 mode by vertical integration,
-// Nyquist rows zeroed.  Spectra layout [level][jy][kx], kx < K.
+// press_stag_array.f90:186-234 + tridag_array.f90:166-246: the z-tridiagonal
+// pressure solve per (kx, ky) column in FP64, the kx = ky = 0 mode by
+// vertical integration, Nyquist rows zeroed.  Spectra layout [level][jy][kx].
+//
+// The pivots of the Thomas elimination depend only on (kx, ky, dz), so
+// ibet_j = 1/bet_j and gam_j are computed once per grid (host, FP64, the
+// reference's recurrence) and a zero pivot is reported when the solver is
+// created.  Each column's sweeps are split into SEG segments worked on by
+// SEG threads: a first pass per segment composes the affine map from the
+// segment's input value to its end value, shared memory chains the maps
+// across segments, and a second pass re-sweeps every segment from its exact
+// input in the reference's order: u_j = (r_j - a_j u_{j-1}) / bet_j forward,
+// u_j = u_j - gam_{j+1} u_{j+1} backward.
 // ---------------------------------------------------------------------------
+constexpr int kThomasSeg = 8;     // segments per column
+constexpr int kThomasCols = 32;   // columns per block (one warp per segment row)
+
 struct ThomasArgs {
-  const double2 *Hx, *Hy, *Hz;   // levels 1..nz at index level-1
-  const double2 *Hb, *Ht;        // r2c of divtz(1), divtz(nz) (scaled)
-  double2* phat;                 // levels 0..nz
-  double* gam;                   // index m*P, m = 0..nz+1
+  const double2 *Hx, *Hy, *Hz;   // levels 1..nz at index level-1, [inst][nz][P]
+  const double2 *Hb, *Ht;        // r2c of divtz(1), divtz(nz) (scaled), [inst][2][P]
+  double2* phat;                 // levels 0..nz, [inst][nz+1][P]; holds r, then u
+  const double *ibet, *gam;      // [n+1][P], index j = 1..n (shared by instances)
   const double *kxw, *kyw;
   double dz;
   int nz, ny, K, ninst;
-  int* err;
 };
 
-__global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
-  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__device__ __forceinline__ double2 thomas_rhs(const ThomasArgs& a, const double2* Hx, const double2* Hy,
+                                              const double2* Hz, const double2* Hb, const double2* Ht, int j,
+                                              long long P, int t, double kxv, double kyv) {
+  const int nz = a.nz;
+  if (j == 1) { const double2 h = Hb[t]; return make_double2(-a.dz * h.x, -a.dz * h.y); }
+  if (j == nz + 1) { const double2 h = Ht[t]; return make_double2(-a.dz * h.x, -a.dz * h.y); }
+  const double c4 = 1.0 / a.dz;
+  const double2 hx = Hx[(j - 2) * P + t], hy = Hy[(j - 2) * P + t];
+  const double2 hz = Hz[(j - 1) * P + t], hzp = Hz[(j - 2) * P + t];
+  // i kx Hx(j-1) + i ky Hy(j-1) + (Hz(j) - Hz(j-1)) / dz
+  return make_double2((-hx.y * kxv) + (-hy.y * kyv) + (hz.x - hzp.x) * c4,
+                      (hx.x * kxv) + (hy.x * kyv) + (hz.y - hzp.y) * c4);
+}
+
+__global__ void __launch_bounds__(kThomasCols * kThomasSeg) k_thomas(ThomasArgs a) {
+  __shared__ double2 s_x[kThomasSeg][kThomasCols];   // segment end value / start value
+  __shared__ double s_h[kThomasSeg][kThomasCols];    // segment map slope
+  const int lane = threadIdx.x % kThomasCols, seg = threadIdx.x / kThomasCols;
   const long long P = (long long)a.ny * a.K;
-  if (gt >= P * a.ninst) return;
-  const int inst = (int)(gt / P);
-  const int t = (int)(gt - inst * P);
+  const long long gcol = (long long)blockIdx.x * kThomasCols + lane;
+  const bool live = gcol < P * a.ninst;
+  const int inst = live ? (int)(gcol / P) : 0;
+  const int t = live ? (int)(gcol - inst * P) : 0;
   const int jy = t / a.K, kx = t - jy * a.K;
   const int nz = a.nz, n = nz + 1;
-  const double dz = a.dz;
-  // per-instance views: H* [inst][nz][P], Hb/Ht [inst][2][P], phat [inst][nz+1][P], gam [inst][nz+2][P]
   const double2* Hx = a.Hx + (long long)inst * nz * P;
   const double2* Hy = a.Hy + (long long)inst * nz * P;
   const double2* Hz = a.Hz + (long long)inst * nz * P;
   const double2* Hb = a.Hb + (long long)inst * 2 * P;
   const double2* Ht = a.Ht + (long long)inst * 2 * P;
-  double2* phat = a.phat + (long long)inst * (nz + 1) * P;
-  double* gam = a.gam + (long long)inst * (nz + 2) * P;
-  if (jy == a.ny / 2) {
-    for (int l = 0; l <= nz; ++l) phat[l * P + t] = make_double2(0.0, 0.0);
-    return;
+  double2* phat = a.phat + (long long)inst * (nz + 1) * P;   // u_j at phat[(j-1)*P]
+  const bool nyq = jy == a.ny / 2;
+  const bool mean = kx == 0 && jy == 0;
+  const int L = (n + kThomasSeg - 1) / kThomasSeg;
+  const int j0 = 1 + seg * L, j1 = min(n, j0 + L - 1);   // this thread's levels (may be empty)
+  const double c3 = 1.0 / (a.dz * a.dz);
+  const double kxv = a.kxw[kx], kyv = a.kyw[jy];
+  const bool solve = live && !nyq && !mean;
+
+  // ---- forward: r_j into phat, and the segment's map x -> u_{j1} = ut + h x
+  double2 ut = make_double2(0.0, 0.0);
+  double h = 1.0;
+  if (solve) {
+    for (int j = j0; j <= j1; ++j) {
+      const double2 r = thomas_rhs(a, Hx, Hy, Hz, Hb, Ht, j, P, t, kxv, kyv);
+      phat[(j - 1) * P + t] = r;
+      const double ib = a.ibet[(long long)j * P + t];
+      const double aj = (j == 1) ? 0.0 : (j <= nz ? c3 : -1.0);
+      ut = make_double2((r.x - aj * ut.x) * ib, (r.y - aj * ut.y) * ib);
+      h = -aj * ib * h;
+    }
   }
-  if (kx == 0 && jy == 0) {
+  s_x[seg][lane] = ut;
+  s_h[seg][lane] = h;
+  __syncthreads();
+  double2 x = make_double2(0.0, 0.0);   // u_{j0-1}
+  for (int s = 0; s < seg; ++s) {
+    const double2 e = s_x[s][lane];
+    const double hs = s_h[s][lane];
+    x = make_double2(e.x + hs * x.x, e.y + hs * x.y);
+  }
+  __syncthreads();
+  // ---- forward re-sweep from the exact input; the segment end is u_{j1}
+  double2 up = x;
+  if (solve) {
+    for (int j = j0; j <= j1; ++j) {
+      const double2 r = phat[(j - 1) * P + t];
+      const double ib = a.ibet[(long long)j * P + t];
+      const double aj = (j == 1) ? 0.0 : (j <= nz ? c3 : -1.0);
+      up = make_double2((r.x - aj * up.x) * ib, (r.y - aj * up.y) * ib);
+      phat[(j - 1) * P + t] = up;
+    }
+  }
+  // ---- backward: v_j = u_j - gam_{j+1} v_{j+1}; map y = v_{j1+1} -> v_{j0} = vt + g y
+  double2 vt = make_double2(0.0, 0.0);
+  double g = 1.0;
+  if (solve) {
+    for (int j = j1; j >= j0; --j) {
+      const double2 uj = phat[(j - 1) * P + t];
+      const double gj = (j == n) ? 0.0 : a.gam[(long long)(j + 1) * P + t];
+      vt = make_double2(uj.x - gj * vt.x, uj.y - gj * vt.y);
+      g = -gj * g;
+    }
+  }
+  s_x[seg][lane] = vt;
+  s_h[seg][lane] = g;
+  __syncthreads();
+  double2 y = make_double2(0.0, 0.0);   // v_{j1+1}; the top segment has none
+  for (int s = kThomasSeg - 1; s > seg; --s) {
+    const double2 e = s_x[s][lane];
+    const double gs = s_h[s][lane];
+    y = make_double2(e.x + gs * y.x, e.y + gs * y.y);
+  }
+  if (solve) {
+    double2 vn = y;
+    for (int j = j1; j >= j0; --j) {
+      double2 uj = phat[(j - 1) * P + t];
+      if (j < n) {
+        const double gj = a.gam[(long long)(j + 1) * P + t];
+        uj = make_double2(uj.x - gj * vn.x, uj.y - gj * vn.y);
+      }
+      phat[(j - 1) * P + t] = uj;
+      vn = uj;
+    }
+  }
+  if (!live) return;
+  if (nyq) {
+    for (int j = j0; j <= j1; ++j) phat[(j - 1) * P + t] = make_double2(0.0, 0.0);
+  } else if (mean && seg == 0) {
+    // kx = ky = 0: p(0) = 0, p(1) = -dz rbottomw, p(jz) = p(jz-1) + Hz(jz) dz
     double2 p = make_double2(0.0, 0.0);
     phat[t] = p;
     const double2 hb = Hb[t];
-    p = make_double2(p.x - dz * hb.x, p.y - dz * hb.y);
+    p = make_double2(p.x - a.dz * hb.x, p.y - a.dz * hb.y);
     phat[P + t] = p;
     for (int jz = 2; jz <= nz; ++jz) {
       const double2 hz = Hz[(jz - 1) * P + t];
-      p = make_double2(p.x + hz.x * dz, p.y + hz.y * dz);
+      p = make_double2(p.x + hz.x * a.dz, p.y + hz.y * a.dz);
       phat[jz * P + t] = p;
     }
-    return;
-  }
-  const double c3 = 1.0 / (dz * dz);
-  const double c4 = 1.0 / dz;
-  const double kxv = a.kxw[kx], kyv = a.kyw[jy];
-  const double bmid = -(kxv * kxv + kyv * kyv + 2.0 * c3);
-  // m = 1: b = -1, c = 1, r = -dz * rbottomw
-  const double2 hb = Hb[t];
-  double2 up = make_double2((-dz * hb.x) / -1.0, (-dz * hb.y) / -1.0);
-  phat[t] = up;
-  double bet = -1.0;
-  double2 hzp = Hz[t];   // level 1
-  for (int j = 2; j <= n; ++j) {
-    double aj, bj, r_x, r_y;
-    const double cprev = (j == 2) ? 1.0 : c3;
-    if (j <= nz) {
-      aj = c3; bj = bmid;
-      const double2 hx = Hx[(j - 2) * P + t], hy = Hy[(j - 2) * P + t];
-      const double2 hz = Hz[(j - 1) * P + t];
-      // i kx Hx + i ky Hy + (Hz(j) - Hz(j-1)) / dz
-      r_x = (-hx.y * kxv) + (-hy.y * kyv) + (hz.x - hzp.x) * c4;
-      r_y = (hx.x * kxv) + (hy.x * kyv) + (hz.y - hzp.y) * c4;
-      hzp = hz;
-    } else {
-      aj = -1.0; bj = 1.0;
-      const double2 ht = Ht[t];
-      r_x = -dz * ht.x; r_y = -dz * ht.y;
-    }
-    const double g = cprev / bet;
-    bet = bj - aj * g;
-    if (bet == 0.0) { atomicExch(a.err, 1); bet = 1.0; }
-    up = make_double2((r_x - aj * up.x) / bet, (r_y - aj * up.y) / bet);
-    gam[j * P + t] = g;
-    phat[(j - 1) * P + t] = up;
-  }
-  double2 un = up;   // u(n)
-  for (int j = n - 1; j >= 1; --j) {
-    const double g = gam[(j + 1) * P + t];
-    double2 uj = phat[(j - 1) * P + t];
-    uj = make_double2(uj.x - g * un.x, uj.y - g * un.y);
-    phat[(j - 1) * P + t] = uj;
-    un = uj;
   }
 }
 

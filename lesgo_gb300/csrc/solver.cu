@@ -358,8 +358,8 @@ static long long footprint_bytes(const Derived& d, int cap) {
   b += (LESGO_NFIELDS + 4 + (d.turbines.empty() ? 0 : 1)) * nf * rs;   // fields, interpolation temps, fza on uv
   b += 4 * plane * rs + 6 * (long long)(d.nz + 1) * pbig * rs;          // wall planes, 3/2-grid fields
   b += (std::max({21 * vs, 6 * vs, 3 * vb}) + std::max({42 * vs, 6 * vb, 9 * vs}) + 4 * ps) * 2 * rs;   // spectra
-  b += (3 * vs + 2 * ps + (long long)(d.nz + 1) * ps) * 16 + (long long)(d.nz + 2) * ps * 8;           // FP64 pressure
-  return b * cap;
+  b += (3 * vs + 2 * ps + (long long)(d.nz + 1) * ps) * 16;                                          // FP64 pressure
+  return b * cap + 2LL * (d.nz + 2) * ps * 8;                                                       // Thomas pivots
 }
 
 template <typename R>
@@ -401,7 +401,7 @@ class Solver : public SolverBase {
     hspec_ = alloc<double2>(3 * vol1_s_ * cap_);
     hplane_ = alloc<double2>(2 * pl_s * cap_);
     phat_ = alloc<double2>((nz + 1) * pl_s * cap_);
-    gam_ = alloc<double>((nz + 2) * pl_s * cap_);
+    build_thomas_pivots();
     err_ = alloc<int>(1);
     zo_d_ = alloc<double>(cap_);
     flags_d_ = alloc<int>(cap_);
@@ -1038,6 +1038,42 @@ class Solver : public SolverBase {
     return p;
   }
 
+  // Thomas pivots of every (kx, ky) column (tridag_array.f90:166-246): they
+  // depend only on the wavenumbers and dz, so they are formed once in FP64.
+  void build_thomas_pivots() {
+    const int ny = d_.ny, K = d_.K, nz = d_.nz, n = nz + 1;
+    const long long P = (long long)ny * K;
+    std::vector<double> ib((size_t)(n + 1) * P, 1.0), gm((size_t)(n + 1) * P, 0.0);
+    const double c3 = 1.0 / (d_.dz * d_.dz);
+    for (int jy = 0; jy < ny; ++jy) {
+      if (jy == ny / 2) continue;
+      const int m = ((jy + ny / 2) % ny) - ny / 2;
+      const double kyv = 2.0 * kPi / d_.p.L_y * (double)m;
+      for (int jx = 0; jx < K; ++jx) {
+        if (jx == 0 && jy == 0) continue;
+        const double kxv = 2.0 * kPi / d_.p.L_x * (double)jx;
+        const long long t = (long long)jy * K + jx;
+        volatile double k2 = kxv * kxv;
+        k2 = k2 + kyv * kyv;
+        const double bmid = -(k2 + 2.0 * c3);
+        double bet = -1.0;
+        ib[P + t] = 1.0 / bet;
+        for (int j = 2; j <= n; ++j) {
+          const double cprev = (j == 2) ? 1.0 : c3;
+          const double aj = (j <= nz) ? c3 : -1.0;
+          const double bj = (j <= nz) ? bmid : 1.0;
+          const double g = cprev / bet;
+          bet = bj - aj * g;
+          if (bet == 0.0) throw Error(LESGO_ERR_NUMERIC, "tridag_array: zero pivot");
+          gm[(size_t)j * P + t] = g;
+          ib[(size_t)j * P + t] = 1.0 / bet;
+        }
+      }
+    }
+    ibet_ = upload_vec(ib);
+    tgam_ = upload_vec(gm);
+  }
+
   void build_tables() {
     px_ = make_plan(d_.nx / 2);
     py_ = make_plan(d_.ny);
@@ -1312,11 +1348,11 @@ class Solver : public SolverBase {
     ThomasArgs ta;
     ta.Hx = hspec_; ta.Hy = hspec_ + vs; ta.Hz = hspec_ + 2 * vs;
     ta.Hb = hplane_; ta.Ht = hplane_ + pl_s;
-    ta.phat = phat_; ta.gam = gam_;
+    ta.phat = phat_; ta.ibet = ibet_; ta.gam = tgam_;
     ta.kxw = kxw64_; ta.kyw = kyw64_;
-    ta.dz = d_.dz; ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.ninst = kp_.ninst; ta.err = err_;
+    ta.dz = d_.dz; ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.ninst = kp_.ninst;
     pre();
-    k_thomas<<<(unsigned)((pl_s * kp_.ninst + 127) / 128), 128, 0, st_>>>(ta);
+    k_thomas<<<(unsigned)((pl_s * kp_.ninst + kThomasCols - 1) / kThomasCols), kThomasCols * kThomasSeg, 0, st_>>>(ta);
     post("press.thomas", (double)pl_s * kp_.ninst * (4.0 * nz + 1.0) * sizeof(double2));
     // p, i kx p, i ky p at levels 1..nz-1; p at levels 0 and nz (phat holds nz+1 planes per instance)
     ypass_lin<1, 3, false, true, double2, T2>(phat_, 1, 1, nz + 1, ny, specB_, ny, nz - 1, 1, ROW_SAME,
@@ -1375,7 +1411,7 @@ class Solver : public SolverBase {
   R* fza_uv_ = nullptr;
   T2 *specA_ = nullptr, *specB_ = nullptr, *specC_ = nullptr;
   double2 *hspec_ = nullptr, *hplane_ = nullptr, *phat_ = nullptr;
-  double* gam_ = nullptr;
+  double *ibet_ = nullptr, *tgam_ = nullptr;
   int* err_ = nullptr;
   double* zo_d_ = nullptr;
   int* flags_d_ = nullptr;
