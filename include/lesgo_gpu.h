@@ -235,6 +235,28 @@ int lesgo_gpu_turbine_state_inst(lesgo_handle_t* h, int id, double* u_d_T, doubl
 /* Device bytes a handle of this grid and capacity allocates (admission). */
 int lesgo_gpu_footprint(const lesgo_params_t* p, int capacity, long long* bytes);
 
+/* ---- time-averaging statistics (time_average.f90; schedule io.f90:557-580)
+ * After every step, per instance: steps jt_total in [nstart, nend] add dt to
+ * the pending weight; a step with (jt_total - nstart) % nskip == 0 starts the
+ * sums (first time, tavg%init) or adds the fields times the pending weight
+ * (tavg%compute).  Sums are FP64 on the device, levels 1..nz.  `which`
+ * selects an average: 0 u, 1 v, 2 w, 3 u_w, 4 v_w, 5 w_uv, 6 u2, 7 v2, 8 w2,
+ * 9 uv, 10 uw, 11 vw, 12 txx, 13 tyy, 14 tzz, 15 txy, 16 txz, 17 tyz,
+ * 18 p (real pressure), 19 fx, 20 fy, 21 fz, 22 cs_opt2, 23 vortx, 24 vorty,
+ * 25 vortz; or a Reynolds stress (time_average.f90:616-629): 26 up2, 27 vp2,
+ * 28 wp2, 29 upvp, 30 upwp, 31 vpwp.  Fields are (ld, ny, lbz..nzhi) like
+ * lesgo_gpu_get_field. */
+int lesgo_gpu_tavg_config(lesgo_handle_t* h, int nstart, int nend, int nskip);
+/* Apply the schedule once now (for callers driving the stage entry points). */
+int lesgo_gpu_tavg_sample(lesgo_handle_t* h);
+int lesgo_gpu_tavg_get(lesgo_handle_t* h, int which, double* host, int lbz, int nzhi);
+int lesgo_gpu_tavg_get_inst(lesgo_handle_t* h, int id, int which, double* host, int lbz, int nzhi);
+/* Plane (x-y) mean of an average at levels 0..nz: prof[n >= nz+1]. */
+int lesgo_gpu_tavg_profile(lesgo_handle_t* h, int which, double* prof, int n);
+int lesgo_gpu_tavg_profile_inst(lesgo_handle_t* h, int id, int which, double* prof, int n);
+/* tavg%total_time of instance id (id < 0: the handle's single instance). */
+int lesgo_gpu_tavg_total_time(lesgo_handle_t* h, int id, double* total_time);
+
 /* ---- instrumentation (no reference counterpart; the reference only
  * prints wall-clock times, main.f90:359-436) --------------------------- */
 /* enable != 0: run steps eagerly (no graph replay) with a CUDA event pair

@@ -105,6 +105,13 @@ SIGNATURES = {
     "lesgo_gpu_counters_inst": (_I, [_H, _I, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_turbine_state_inst": (_I, [_H, _I, _D, _D, _D, _I]),
     "lesgo_gpu_footprint": (_I, [C.POINTER(Params), _I, C.POINTER(C.c_longlong)]),
+    "lesgo_gpu_tavg_config": (_I, [_H, _I, _I, _I]),
+    "lesgo_gpu_tavg_sample": (_I, [_H]),
+    "lesgo_gpu_tavg_get": (_I, [_H, _I, _D, _I, _I]),
+    "lesgo_gpu_tavg_get_inst": (_I, [_H, _I, _I, _D, _I, _I]),
+    "lesgo_gpu_tavg_profile": (_I, [_H, _I, _D, _I]),
+    "lesgo_gpu_tavg_profile_inst": (_I, [_H, _I, _I, _D, _I]),
+    "lesgo_gpu_tavg_total_time": (_I, [_H, _I, _D]),
     "lesgo_gpu_profile": (_I, [_H, _I]),
     "lesgo_gpu_profile_report": (_I, [_H, C.c_char_p, _I]),
     "lesgo_gpu_get_stream": (_I, [_H, C.POINTER(C.c_void_p)]),

@@ -866,3 +866,102 @@ __global__ void __launch_bounds__(128) k_tridag(const double* __restrict__ a, co
 }
 
 }  // namespace lesgo
+
+namespace lesgo {
+
+// ---------------------------------------------------------------------------
+// Time-averaging statistics (time_average.f90:176-319): 26 FP64 accumulators
+// per instance, each sample weighted by the time since the previous sample.
+// ---------------------------------------------------------------------------
+enum : int {
+  TA_U = 0, TA_V, TA_W, TA_U_W, TA_V_W, TA_W_UV, TA_U2, TA_V2, TA_W2, TA_UV, TA_UW, TA_VW,
+  TA_TXX, TA_TYY, TA_TZZ, TA_TXY, TA_TXZ, TA_TYZ, TA_P, TA_FX, TA_FY, TA_FZ, TA_CS, TA_VORTX, TA_VORTY,
+  TA_VORTZ, TA_N
+};
+
+template <typename R>
+struct TavgArgs {
+  const R *u, *v, *w, *p, *txx, *tyy, *tzz, *txy, *txz, *tyz, *fxa, *fya, *fza, *cs;
+  const R *dudy, *dudz, *dvdx, *dvdz, *dwdx, *dwdy;
+  double* acc;            // [TA_N][inst][nz+1][ny][ld]
+  long long acc_stride;   // elements between quantities
+  const double* wgt;      // per-instance sample weight (0: no sample)
+  KP kp;
+};
+
+template <typename R>
+__global__ void k_tavg(TavgArgs<R> a) {
+  const KP& kp = a.kp;
+  const long long n = (long long)kp.nx * kp.ny * kp.nz * kp.ninst;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const PtIdx x = pt_index(t, kp);
+  const double wt = a.wgt[x.inst];
+  if (wt == 0.0) return;
+  const int k = x.k, nz = kp.nz;
+  const long long q = x.q, P = kp.plane;
+  const double u = a.u[q], v = a.v[q], w = a.w[q];
+  // interp_to_uv_grid (functions.f90:51-105): level nz repeats nz-1
+  const long long qu = (k == nz) ? q - P : q;
+  const double w_uv = 0.5 * ((double)a.w[qu + P] + (double)a.w[qu]);
+  // interp_to_w_grid (functions.f90:108-185); zero at a wall (time_average.f90:227-232)
+  double u_w = 0.0, v_w = 0.0, vortz = 0.0;
+  if (k >= 2) {
+    u_w = 0.5 * ((double)a.u[q - P] + (double)a.u[q]);
+    v_w = 0.5 * ((double)a.v[q - P] + (double)a.v[q]);
+    vortz = 0.5 * (((double)a.dvdx[q - P] - (double)a.dudy[q - P]) + ((double)a.dvdx[q] - (double)a.dudy[q]));
+  }
+  if (k == nz && kp.ubc > 0) { u_w = 0.0; v_w = 0.0; }
+  if (k == 1 && kp.lbc > 0) { u_w = 0.0; v_w = 0.0; }
+  const double pres = (double)a.p[q] - 0.5 * (u * u + w_uv * w_uv + v * v);
+  double fz_uv = 0.0;
+  if (kp.turbines) fz_uv = 0.5 * ((double)a.fza[qu + P] + (double)a.fza[qu]);
+  const double vals[TA_N] = {
+      u, v, w, u_w, v_w, w_uv, u * u, v * v, w * w, u * v, u_w * w, v_w * w,
+      (double)a.txx[q], (double)a.tyy[q], (double)a.tzz[q], (double)a.txy[q], (double)a.txz[q], (double)a.tyz[q],
+      pres, kp.turbines ? (double)a.fxa[q] : 0.0, kp.turbines ? (double)a.fya[q] : 0.0, fz_uv, (double)a.cs[q],
+      (double)a.dwdy[q] - (double)a.dvdz[q], (double)a.dudz[q] - (double)a.dwdx[q], vortz};
+#pragma unroll
+  for (int f = 0; f < TA_N; ++f) a.acc[f * a.acc_stride + q] += vals[f] * wt;
+}
+
+// The time average of quantity `which` (accumulator / total time), or a
+// Reynolds stress (time_average.f90:616-629): 26 u'u', 27 v'v', 28 w'w',
+// 29 u'v', 30 u'w' (w grid), 31 v'w' (w grid).  One instance, levels 0..nz.
+__global__ void k_tavg_get(const double* acc, long long acc_stride, long long ib, int which, double inv_t,
+                           double* out, long long n) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  auto A = [&](int f) { return acc[f * acc_stride + ib + t] * inv_t; };
+  double r;
+  switch (which) {
+    case TA_N + 0: r = A(TA_U2) - A(TA_U) * A(TA_U); break;
+    case TA_N + 1: r = A(TA_V2) - A(TA_V) * A(TA_V); break;
+    case TA_N + 2: r = A(TA_W2) - A(TA_W) * A(TA_W); break;
+    case TA_N + 3: r = A(TA_UV) - A(TA_U) * A(TA_V); break;
+    case TA_N + 4: r = A(TA_UW) - A(TA_U_W) * A(TA_W); break;
+    case TA_N + 5: r = A(TA_VW) - A(TA_V_W) * A(TA_W); break;
+    default: r = A(which);
+  }
+  out[t] = r;
+}
+
+// Plane mean over x < nx of a (ld, ny, levels) double array: one block per level.
+__global__ void k_plane_mean(const double* f, int nx, int ny, int ld, double* out) {
+  __shared__ double sh[256];
+  const long long base = (long long)blockIdx.x * ny * ld;
+  double s = 0.0;
+  for (int t = threadIdx.x; t < nx * ny; t += blockDim.x) {
+    const int j = t / nx, i = t - j * nx;
+    s += f[base + (long long)j * ld + i];
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0] / ((double)nx * ny);
+}
+
+}  // namespace lesgo

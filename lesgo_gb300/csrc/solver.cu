@@ -346,6 +346,11 @@ class SolverBase {
   virtual void* stream() const = 0;
   virtual int tridag(const double* a, const double* b, const double* c, const double* r, double* u, int lh, int ny,
                      int n) = 0;
+  virtual void tavg_config(int nstart, int nend, int nskip) = 0;
+  virtual void tavg_sample() = 0;
+  virtual void tavg_get(int id, int which, double* host, int lbz, int nzhi) = 0;
+  virtual void tavg_profile(int id, int which, double* prof, int n) = 0;
+  virtual double tavg_total_time(int id) const = 0;
 };
 
 // Device bytes of a handle (the admission footprint of a batch).
@@ -453,6 +458,10 @@ class Solver : public SolverBase {
       for (int f = 0; f < LESGO_NFIELDS; ++f)
         CK(cudaMemcpyAsync(F_[f] + slot * kp_.istride, F_[f] + last * kp_.istride, kp_.istride * sizeof(R),
                            cudaMemcpyDeviceToDevice, st_));
+      if (tacc_)
+        for (int f = 0; f < TA_N; ++f)
+          CK(cudaMemcpyAsync(tacc_ + f * tacc_stride_ + slot * kp_.istride, tacc_ + f * tacc_stride_ + last * kp_.istride,
+                             kp_.istride * sizeof(double), cudaMemcpyDeviceToDevice, st_));
       slots_[slot] = slots_[last];
     }
     const bool had_turbines = kp_.turbines != 0;
@@ -688,8 +697,98 @@ class Solver : public SolverBase {
         if (!special) launch_count_[lag_any ? 1 : 0] = launches_;
       }
       commit_lagrange_init();
+      if (tavg_on_) tavg_sample();
     }
   }
+
+  // ---------------- time averaging (time_average.f90, io.f90:557-580) --------
+  void tavg_config(int nstart, int nend, int nskip) override {
+    if (nskip < 1 || nend < nstart) throw Error(LESGO_ERR_ARG, "tavg: need nskip >= 1 and nend >= nstart");
+    if (!tacc_) {
+      tacc_stride_ = kp_.istride * cap_;
+      tacc_ = alloc<double>(TA_N * tacc_stride_);
+      tw_d_ = alloc<double>(cap_);
+    }
+    CK(cudaMemsetAsync(tacc_, 0, TA_N * tacc_stride_ * sizeof(double), st_));
+    ta_nstart_ = nstart; ta_nend_ = nend; ta_nskip_ = nskip;
+    tavg_on_ = true;
+    for (auto& sl : slots_) { sl.ta_init = false; sl.ta_dt = 0.0; sl.ta_total = 0.0; }
+    CK(cudaStreamSynchronize(st_));
+  }
+  // output_loop's schedule for each instance after a step: every step of
+  // [nstart, nend] adds dt; the first sample step starts the sums, later ones
+  // add the fields weighted by the time since the previous sample.
+  void tavg_sample() override {
+    if (!tavg_on_) throw Error(LESGO_ERR_ARG, "tavg: not configured");
+    need_active();
+    std::vector<double> w(slots_.size(), 0.0);
+    bool any = false;
+    for (size_t s = 0; s < slots_.size(); ++s) {
+      Slot& sl = slots_[s];
+      if (sl.jt_total < ta_nstart_ || sl.jt_total > ta_nend_) continue;
+      sl.ta_dt += d_.p.dt;
+      if ((sl.jt_total - ta_nstart_) % ta_nskip_ != 0) continue;
+      if (!sl.ta_init) {
+        for (int f = 0; f < TA_N; ++f)
+          CK(cudaMemsetAsync(tacc_ + f * tacc_stride_ + s * kp_.istride, 0, kp_.istride * sizeof(double), st_));
+        sl.ta_init = true;
+        sl.ta_total = 0.0;
+        sl.ta_dt = 0.0;
+      } else {
+        w[s] = sl.ta_dt;
+        sl.ta_total += sl.ta_dt;
+        sl.ta_dt = 0.0;
+        any = true;
+      }
+    }
+    if (!any) return;
+    CK(cudaMemcpyAsync(tw_d_, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, st_));
+    TavgArgs<R> a;
+    a.u = F_[LESGO_U]; a.v = F_[LESGO_V]; a.w = F_[LESGO_W]; a.p = F_[LESGO_P];
+    a.txx = F_[LESGO_TXX]; a.tyy = F_[LESGO_TYY]; a.tzz = F_[LESGO_TZZ];
+    a.txy = F_[LESGO_TXY]; a.txz = F_[LESGO_TXZ]; a.tyz = F_[LESGO_TYZ];
+    a.fxa = F_[LESGO_FXA]; a.fya = F_[LESGO_FYA]; a.fza = F_[LESGO_FZA]; a.cs = F_[LESGO_CS_OPT2];
+    a.dudy = F_[LESGO_DUDY]; a.dudz = F_[LESGO_DUDZ]; a.dvdx = F_[LESGO_DVDX]; a.dvdz = F_[LESGO_DVDZ];
+    a.dwdx = F_[LESGO_DWDX]; a.dwdy = F_[LESGO_DWDY];
+    a.acc = tacc_; a.acc_stride = tacc_stride_; a.wgt = tw_d_; a.kp = kp_;
+    const long long n = (long long)d_.nx * d_.ny * d_.nz * kp_.ninst;
+    pre();
+    k_tavg<R><<<grid1(n), 256, 0, st_>>>(a);
+    post("tavg.compute", (double)n * (20.0 * sizeof(R) + 2.0 * TA_N * 8));
+  }
+  void tavg_get(int id, int which, double* host, int lbz, int nzhi) override {
+    if (!tacc_) throw Error(LESGO_ERR_ARG, "tavg: not configured");
+    if (which < 0 || which >= TA_N + 6) throw Error(LESGO_ERR_ARG, "tavg: bad quantity");
+    if (lbz < 0 || nzhi > d_.nz || nzhi < lbz) throw Error(LESGO_ERR_ARG, "levels outside 0..nz");
+    const int slot = slot_of(id);
+    const Slot& sl = slots_[slot];
+    if (!(sl.ta_total > 0)) throw Error(LESGO_ERR_ARG, "tavg: no sample yet");
+    double* stg = staging(kp_.istride);
+    const long long n = kp_.istride;
+    k_tavg_get<<<grid1(n), 256, 0, st_>>>(tacc_, tacc_stride_, slot * kp_.istride, which, 1.0 / sl.ta_total, stg, n);
+    post();
+    const long long off = (long long)lbz * kp_.plane, cnt = (long long)(nzhi - lbz + 1) * kp_.plane;
+    CK(cudaMemcpyAsync(host, stg + off, cnt * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+  }
+  void tavg_profile(int id, int which, double* prof, int n) override {
+    if (n < d_.nz + 1) throw Error(LESGO_ERR_ARG, "tavg_profile: need nz+1 values");
+    if (!tacc_) throw Error(LESGO_ERR_ARG, "tavg: not configured");
+    if (which < 0 || which >= TA_N + 6) throw Error(LESGO_ERR_ARG, "tavg: bad quantity");
+    const int slot = slot_of(id);
+    const Slot& sl = slots_[slot];
+    if (!(sl.ta_total > 0)) throw Error(LESGO_ERR_ARG, "tavg: no sample yet");
+    double* stg = staging(kp_.istride);
+    if (!prof_d_) prof_d_ = alloc<double>(d_.nz + 1);
+    k_tavg_get<<<grid1(kp_.istride), 256, 0, st_>>>(tacc_, tacc_stride_, slot * kp_.istride, which, 1.0 / sl.ta_total,
+                                                    stg, kp_.istride);
+    post();
+    k_plane_mean<<<d_.nz + 1, 256, 0, st_>>>(stg, d_.nx, d_.ny, d_.ld, prof_d_);
+    post();
+    CK(cudaMemcpyAsync(prof, prof_d_, (d_.nz + 1) * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+  }
+  double tavg_total_time(int id) const override { return slots_[slot_of(id)].ta_total; }
 
   int sync() override {
     CK(cudaStreamSynchronize(st_));
@@ -815,6 +914,8 @@ class Solver : public SolverBase {
     int jt = 0, jt_total = 0;
     bool flm_init = false, fqn_init = false;
     int pending = 0;   // IF_INITLM / IF_INITQN set this step (committed after it)
+    bool ta_init = false;          // time averaging started (tavg%init done)
+    double ta_dt = 0.0, ta_total = 0.0;
   };
 
   int slot_of(int id) const {
@@ -1412,6 +1513,10 @@ class Solver : public SolverBase {
   T2 *specA_ = nullptr, *specB_ = nullptr, *specC_ = nullptr;
   double2 *hspec_ = nullptr, *hplane_ = nullptr, *phat_ = nullptr;
   double *ibet_ = nullptr, *tgam_ = nullptr;
+  double *tacc_ = nullptr, *tw_d_ = nullptr, *prof_d_ = nullptr;
+  long long tacc_stride_ = 0;
+  bool tavg_on_ = false;
+  int ta_nstart_ = 1, ta_nend_ = 50000, ta_nskip_ = 100;
   int* err_ = nullptr;
   double* zo_d_ = nullptr;
   int* flags_d_ = nullptr;
@@ -1835,4 +1940,34 @@ int lesgo_gpu_footprint(const lesgo_params_t* p, int capacity, long long* bytes)
   }
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Time-averaging statistics
+// ---------------------------------------------------------------------------
+extern "C" {
+int lesgo_gpu_tavg_config(lesgo_handle_t* h, int nstart, int nend, int nskip) {
+  return guarded(h, [&] { h->s->tavg_config(nstart, nend, nskip); });
+}
+int lesgo_gpu_tavg_sample(lesgo_handle_t* h) { return guarded(h, [&] { h->s->tavg_sample(); }); }
+int lesgo_gpu_tavg_get(lesgo_handle_t* h, int which, double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->tavg_get(h->inst0, which, host, lbz, nzhi); });
+}
+int lesgo_gpu_tavg_get_inst(lesgo_handle_t* h, int id, int which, double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->tavg_get(id, which, host, lbz, nzhi); });
+}
+int lesgo_gpu_tavg_profile(lesgo_handle_t* h, int which, double* prof, int n) {
+  if (!prof) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->tavg_profile(h->inst0, which, prof, n); });
+}
+int lesgo_gpu_tavg_profile_inst(lesgo_handle_t* h, int id, int which, double* prof, int n) {
+  if (!prof) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->tavg_profile(id, which, prof, n); });
+}
+int lesgo_gpu_tavg_total_time(lesgo_handle_t* h, int id, double* t) {
+  if (!t) return LESGO_ERR_ARG;
+  return guarded(h, [&] { *t = h->s->tavg_total_time(id < 0 ? h->inst0 : id); });
+}
 }  // extern "C"

@@ -21,6 +21,13 @@ import numpy as np
 from . import _lib as L
 
 
+# Time-averaged quantities in the order the library numbers them
+# (time_average.f90:176-319), then the Reynolds stresses (:616-629).
+TAVG_QUANTITIES = ["u", "v", "w", "u_w", "v_w", "w_uv", "u2", "v2", "w2", "uv", "uw", "vw",
+                   "txx", "tyy", "tzz", "txy", "txz", "tyz", "p", "fx", "fy", "fz", "cs_opt2",
+                   "vortx", "vorty", "vortz", "up2", "vp2", "wp2", "upvp", "upwp", "vpwp"]
+
+
 class LesgoError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"lesgo_gpu error {code}: {msg}")
@@ -276,6 +283,31 @@ class LesgoGPU:
     def launches_per_step(self, with_sgs_update: bool = False) -> int:
         return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
 
+    # ---------------- time averaging ---------------------------------------------------
+    def tavg_config(self, nstart: int, nend: int, nskip: int):
+        """tavg_nstart / tavg_nend / tavg_nskip of the reference's input."""
+        self._check(self._lib.lesgo_gpu_tavg_config(self._h, nstart, nend, nskip))
+
+    def tavg_sample(self):
+        self._check(self._lib.lesgo_gpu_tavg_sample(self._h))
+
+    def tavg_get(self, name: str, lbz: int = 1) -> np.ndarray:
+        out = np.zeros((self.nz + 1 - lbz, self.ny, self.ld))
+        self._check(self._lib.lesgo_gpu_tavg_get(self._h, TAVG_QUANTITIES.index(name),
+                                                 out.ctypes.data_as(C.POINTER(C.c_double)), lbz, self.nz))
+        return out
+
+    def tavg_profile(self, name: str) -> np.ndarray:
+        out = np.zeros(self.nz + 1)
+        self._check(self._lib.lesgo_gpu_tavg_profile(self._h, TAVG_QUANTITIES.index(name),
+                                                     out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out
+
+    def tavg_total_time(self) -> float:
+        t = C.c_double()
+        self._check(self._lib.lesgo_gpu_tavg_total_time(self._h, -1, C.byref(t)))
+        return t.value
+
 
 class LesgoBatch:
     """A batch of independent LES instances of one grid size on the current
@@ -381,3 +413,28 @@ class LesgoBatch:
 
     def launches_per_step(self, with_sgs_update: bool = False) -> int:
         return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
+
+    # ---------------- time averaging ---------------------------------------------------
+    def tavg_config(self, nstart: int, nend: int, nskip: int):
+        """tavg_nstart / tavg_nend / tavg_nskip of the reference's input."""
+        self._check(self._lib.lesgo_gpu_tavg_config(self._h, nstart, nend, nskip))
+
+    def tavg_sample(self):
+        self._check(self._lib.lesgo_gpu_tavg_sample(self._h))
+
+    def tavg_get(self, iid: int, name: str, lbz: int = 1) -> np.ndarray:
+        out = np.zeros((self.nz + 1 - lbz, self.ny, self.ld))
+        self._check(self._lib.lesgo_gpu_tavg_get_inst(self._h, iid, TAVG_QUANTITIES.index(name),
+                                                 out.ctypes.data_as(C.POINTER(C.c_double)), lbz, self.nz))
+        return out
+
+    def tavg_profile(self, iid: int, name: str) -> np.ndarray:
+        out = np.zeros(self.nz + 1)
+        self._check(self._lib.lesgo_gpu_tavg_profile_inst(self._h, iid, TAVG_QUANTITIES.index(name),
+                                                     out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out
+
+    def tavg_total_time(self, iid: int) -> float:
+        t = C.c_double()
+        self._check(self._lib.lesgo_gpu_tavg_total_time(self._h, iid, C.byref(t)))
+        return t.value

@@ -1237,6 +1237,106 @@ class Oracle:
             fn()
 
 
+# ---------------------------------------------------------------------------
+# Time-averaging statistics: time_average.f90:176-319 (compute), :616-629
+# (Reynolds stresses) and the schedule of io.f90:557-580.  Serial layout:
+# levels 1..nz (lbz = 1).  interp_to_w_grid leaves level 1 unset in a serial
+# run; here it is 0 (the reference zeroes it itself whenever lbc_mom > 0).
+# ---------------------------------------------------------------------------
+TAVG_NAMES = ["u", "v", "w", "u_w", "v_w", "w_uv", "u2", "v2", "w2", "uv", "uw", "vw",
+              "txx", "tyy", "tzz", "txy", "txz", "tyz", "p", "fx", "fy", "fz", "cs_opt2",
+              "vortx", "vorty", "vortz"]
+TAVG_RS_NAMES = ["up2", "vp2", "wp2", "upvp", "upwp", "vpwp"]
+
+
+class TimeAverage:
+    def __init__(self, o: "Oracle", nstart: int, nend: int, nskip: int):
+        self.o = o
+        self.nstart, self.nend, self.nskip = nstart, nend, nskip
+        self.initialized = False
+        self.dt = 0.0
+        self.total_time = 0.0
+        nz, ny, nx = o.p.nz, o.p.ny, o.p.nx
+        self.acc = {n: np.zeros((nz + 1, ny, nx)) for n in TAVG_NAMES}
+
+    def after_step(self):
+        """io.f90:557-580."""
+        jt = self.o.jt_total
+        if self.nstart <= jt <= self.nend:
+            self.dt += self.o.p.dt
+            if (jt - self.nstart) % self.nskip == 0:
+                if not self.initialized:
+                    self.init()
+                else:
+                    self.compute()
+
+    def init(self):
+        for a in self.acc.values():
+            a[:] = 0.0
+        self.total_time = 0.0
+        self.dt = 0.0
+        self.initialized = True
+
+    def sample(self):
+        """The 26 sampled quantities at levels 1..nz (index 0 unused)."""
+        o, p = self.o, self.o.p
+        nx, nz = p.nx, p.nz
+        g = lambda f: f[:, :, :nx]
+        u, v, w, pr = g(o.u), g(o.v), g(o.w), g(o.pres)
+
+        def to_uv(f):                      # functions.f90:51-105
+            r = np.zeros_like(f)
+            r[1:nz] = 0.5 * (f[2:nz + 1] + f[1:nz])
+            r[nz] = r[nz - 1]
+            return r
+
+        def to_w(f):                       # functions.f90:108-185, level 1 left 0
+            r = np.zeros_like(f)
+            r[2:nz + 1] = 0.5 * (f[1:nz] + f[2:nz + 1])
+            return r
+
+        w_uv, u_w, v_w = to_uv(w), to_w(u), to_w(v)
+        vortz = to_w(g(o.dvdx) - g(o.dudy))
+        vortz[1] = 0.0
+        if p.lbc_mom > 0:
+            u_w[1] = 0.0
+            v_w[1] = 0.0
+        if p.ubc_mom > 0:
+            u_w[nz] = 0.0
+            v_w[nz] = 0.0
+        pres = pr - 0.5 * (u ** 2 + w_uv ** 2 + v ** 2)
+        if self.o.farm is not None:
+            fx, fy, fz = g(o.fxa), g(o.fya), to_uv(g(o.fza))
+        else:
+            fx = fy = fz = np.zeros_like(u)
+        vals = dict(u=u, v=v, w=w, u_w=u_w, v_w=v_w, w_uv=w_uv, u2=u * u, v2=v * v, w2=w * w,
+                    uv=u * v, uw=u_w * w, vw=v_w * w, txx=g(o.txx), tyy=g(o.tyy), tzz=g(o.tzz),
+                    txy=g(o.txy), txz=g(o.txz), tyz=g(o.tyz), p=pres, fx=fx, fy=fy, fz=fz,
+                    cs_opt2=g(o.Cs_opt2), vortx=g(o.dwdy) - g(o.dvdz), vorty=g(o.dudz) - g(o.dwdx),
+                    vortz=vortz)
+        for k in vals:
+            vals[k] = vals[k].copy()
+            vals[k][0] = 0.0
+        return vals
+
+    def compute(self):
+        vals = self.sample()
+        for n in TAVG_NAMES:
+            self.acc[n] += vals[n] * self.dt
+        self.total_time += self.dt
+        self.dt = 0.0
+
+    def mean(self, name: str) -> np.ndarray:
+        """Time average of a sampled quantity or a Reynolds stress, (nz+1, ny, nx)."""
+        A = lambda n: self.acc[n] / self.total_time
+        rs = {"up2": ("u2", "u", "u"), "vp2": ("v2", "v", "v"), "wp2": ("w2", "w", "w"),
+              "upvp": ("uv", "u", "v"), "upwp": ("uw", "u_w", "w"), "vpwp": ("vw", "v_w", "w")}
+        if name in rs:
+            a, b, c = rs[name]
+            return A(a) - A(b) * A(c)
+        return A(name)
+
+
 def tridag_array(a, b, c, r, mask):
     """tridag_array.f90:166-246 (serial Thomas algorithm) on all columns.
 
