@@ -97,6 +97,18 @@ typedef struct {
   int adm_correction;
 } lesgo_params_t;
 
+/* The run-control values of lesgo.conf that lesgo_params_t does not carry
+ * (param.f90:100-240): read by lesgo_gpu_read_conf for the caller's loop. */
+typedef struct {
+  int nproc, uniform_spacing, wall_damp_exp, sgs;
+  double Co;
+  int nsteps, runtime, use_cfl_dt;
+  double cfl;
+  int cumulative_time, inilag;
+  int wbase, nenergy, lag_cfl_count, checkpoint_data, checkpoint_nskip;
+  int tavg_calc, tavg_nstart, tavg_nend, tavg_nskip;
+} lesgo_run_t;
+
 typedef struct lesgo_handle lesgo_handle_t;
 
 /* Fill *p with lesgo.conf defaults of the half-channel case (lbc_mom=2,
@@ -256,6 +268,44 @@ int lesgo_gpu_tavg_profile(lesgo_handle_t* h, int which, double* prof, int n);
 int lesgo_gpu_tavg_profile_inst(lesgo_handle_t* h, int id, int which, double* prof, int n);
 /* tavg%total_time of instance id (id < 0: the handle's single instance). */
 int lesgo_gpu_tavg_total_time(lesgo_handle_t* h, int id, double* total_time);
+
+/* ---- configuration (input_util.f90:54-1023 read_input_conf; turbine
+ * placement turbines.f90:740-866) -----------------------------------------
+ * Reads <path>lesgo.conf into *p (reference defaults for absent keys) and
+ * *run.  with_turbines != 0 parses the TURBINES block (else it is skipped
+ * like a build without turbines) and places the disks into turbines[0..max):
+ * p->turbines points there and p->n_turbines counts them; read_param reads
+ * <path>input_turbines/param.dat.  Host only (no device is touched).
+ * Malformed files: LESGO_ERR_ARG with file:line in lesgo_gpu_last_error(NULL);
+ * settings whose physics this library leaves out (coriolis_forcing,
+ * use_sponge, inflow_type, use_random_force, sgs = .false., dynamic or
+ * rotating turbines): LESGO_ERR_UNSUPPORTED.  `log` (may be NULL) receives
+ * the reference's notes on unused blocks and keys. */
+int lesgo_gpu_read_conf(const char* path, int with_turbines, lesgo_params_t* p, lesgo_run_t* run,
+                        lesgo_turbine_t* turbines, int max_turbines, char* log, int loglen);
+
+/* ---- checkpoint / restart (io.f90:1173-1267 checkpoint; initial.f90:20-380
+ * and io.f90:60-96 restart) ------------------------------------------------
+ * `path` is a prefix like the reference's `path` (a directory with its
+ * trailing '/').  Writes <path>vel.out (one Fortran unformatted sequential
+ * record: u, v, w, RHSx, RHSy, RHSz, Cs_opt2, F_LM, F_MM, F_QN, F_NN, each
+ * (ld, ny, 1:nz) FP64), <path>grid.out, <path>total_time.dat and, when time
+ * averaging has started, <path>tavg.out.  mpi_names != 0 names the per-rank
+ * files like an MPI run of one rank (vel.out.c0, tavg.out.c0). */
+int lesgo_gpu_checkpoint_write(lesgo_handle_t* h, const char* path, int mpi_names);
+int lesgo_gpu_checkpoint_write_inst(lesgo_handle_t* h, int id, const char* path, int mpi_names);
+/* Restart from <path>vel.out (or vel.out.c0; vel.out.c<n> per rank of an MPI
+ * checkpoint).  Same grid and one rank (grid.out): every field is taken and
+ * the run continues as initu (no Euler first step, no Lagrangian
+ * initialisation); *same_grid = 1.  Otherwise u, v, w are interpolated onto
+ * this grid (ic_interp) and the other fields start at zero; *same_grid = 0.
+ * total_time.dat, if present, sets jt_total and total_time (jt restarts at
+ * 0).  With time averaging configured, tavg.out's sums are taken up at the
+ * first sample step.  Missing or malformed files: LESGO_ERR_ARG. */
+int lesgo_gpu_checkpoint_read(lesgo_handle_t* h, const char* path, int* same_grid);
+int lesgo_gpu_checkpoint_read_inst(lesgo_handle_t* h, int id, const char* path, int* same_grid);
+/* total_time of instance id (id < 0: the handle's single instance). */
+int lesgo_gpu_sim_time(lesgo_handle_t* h, int id, double* total_time);
 
 /* ---- instrumentation (no reference counterpart; the reference only
  * prints wall-clock times, main.f90:359-436) --------------------------- */

@@ -51,6 +51,15 @@ class Params(C.Structure):
     ]
 
 
+class Run(C.Structure):
+    """lesgo_run_t: run control read from lesgo.conf."""
+    _fields_ = [(n, C.c_int) for n in ("nproc", "uniform_spacing", "wall_damp_exp", "sgs")] + [
+        ("Co", C.c_double)] + [(n, C.c_int) for n in ("nsteps", "runtime", "use_cfl_dt")] + [
+        ("cfl", C.c_double)] + [(n, C.c_int) for n in (
+            "cumulative_time", "inilag", "wbase", "nenergy", "lag_cfl_count", "checkpoint_data", "checkpoint_nskip",
+            "tavg_calc", "tavg_nstart", "tavg_nend", "tavg_nskip")]
+
+
 # exported symbol -> (restype, argtypes); every function include/lesgo_gpu.h declares
 _H = C.c_void_p
 _I = C.c_int
@@ -112,6 +121,13 @@ SIGNATURES = {
     "lesgo_gpu_tavg_profile": (_I, [_H, _I, _D, _I]),
     "lesgo_gpu_tavg_profile_inst": (_I, [_H, _I, _I, _D, _I]),
     "lesgo_gpu_tavg_total_time": (_I, [_H, _I, _D]),
+    "lesgo_gpu_checkpoint_write": (_I, [_H, C.c_char_p, _I]),
+    "lesgo_gpu_checkpoint_write_inst": (_I, [_H, _I, C.c_char_p, _I]),
+    "lesgo_gpu_checkpoint_read": (_I, [_H, C.c_char_p, C.POINTER(_I)]),
+    "lesgo_gpu_checkpoint_read_inst": (_I, [_H, _I, C.c_char_p, C.POINTER(_I)]),
+    "lesgo_gpu_sim_time": (_I, [_H, _I, _D]),
+    "lesgo_gpu_read_conf": (_I, [C.c_char_p, _I, C.POINTER(Params), C.POINTER(Run), C.POINTER(Turbine), _I,
+                                 C.c_char_p, _I]),
     "lesgo_gpu_profile": (_I, [_H, _I]),
     "lesgo_gpu_profile_report": (_I, [_H, C.c_char_p, _I]),
     "lesgo_gpu_get_stream": (_I, [_H, C.POINTER(C.c_void_p)]),

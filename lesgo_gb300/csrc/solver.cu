@@ -4,6 +4,8 @@
 // captured CUDA graphs of the steady steps.
 #include "lesgo_gpu.h"
 #include "kernels.cuh"
+#include "restart_io.hpp"
+#include "conf.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -351,6 +353,9 @@ class SolverBase {
   virtual void tavg_get(int id, int which, double* host, int lbz, int nzhi) = 0;
   virtual void tavg_profile(int id, int which, double* prof, int n) = 0;
   virtual double tavg_total_time(int id) const = 0;
+  virtual void checkpoint_write(int id, const std::string& path, int mpi_names) = 0;
+  virtual int checkpoint_read(int id, const std::string& path) = 0;
+  virtual double sim_time(int id) const = 0;
 };
 
 // Device bytes of a handle (the admission footprint of a batch).
@@ -438,6 +443,7 @@ class Solver : public SolverBase {
     Slot sl;
     sl.id = next_id_++;
     sl.spec = spec;
+    sl.initu = d_.p.initu != 0;
     const int slot = (int)slots_.size();
     slots_.push_back(sl);
     sync_instance_params();
@@ -619,7 +625,7 @@ class Solver : public SolverBase {
   }
   void begin_step() override {
     need_active();
-    for (auto& sl : slots_) { ++sl.jt; ++sl.jt_total; }
+    for (auto& sl : slots_) { ++sl.jt; ++sl.jt_total; sl.time += d_.p.dt; }
     for (int c = 0; c < 3; ++c)
       CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c], F_[LESGO_RHSX + c], kp_.istride * kp_.ninst * sizeof(R),
                          cudaMemcpyDeviceToDevice, st_));
@@ -635,7 +641,7 @@ class Solver : public SolverBase {
   void ab2() override {
     need_active();
     for (int s = 0; s < (int)slots_.size(); ++s)
-      if (slots_[s].jt_total == 1 && !d_.p.initu)
+      if (slots_[s].jt_total == 1 && !slots_[s].initu)
         for (int c = 0; c < 3; ++c)
           CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c] + s * kp_.istride, F_[LESGO_RHSX + c] + s * kp_.istride,
                              kp_.istride * sizeof(R), cudaMemcpyDeviceToDevice, st_));
@@ -666,7 +672,7 @@ class Solver : public SolverBase {
   void step(int nsteps) override {
     need_active();
     for (int s = 0; s < nsteps; ++s) {
-      for (auto& sl : slots_) { ++sl.jt; ++sl.jt_total; }
+      for (auto& sl : slots_) { ++sl.jt; ++sl.jt_total; sl.time += d_.p.dt; }
       bool lag_any = false;
       const bool special = upload_flags(true, &lag_any);
       const int code = (lag_any ? 1 : 0) | (kp_.ninst << 1);
@@ -729,10 +735,14 @@ class Solver : public SolverBase {
       sl.ta_dt += d_.p.dt;
       if ((sl.jt_total - ta_nstart_) % ta_nskip_ != 0) continue;
       if (!sl.ta_init) {
+        // tavg%init: zero sums, or take up the sums read from tavg.out
+        // (which carries no pressure sum: time_average.f90:114-150)
         for (int f = 0; f < TA_N; ++f)
-          CK(cudaMemsetAsync(tacc_ + f * tacc_stride_ + s * kp_.istride, 0, kp_.istride * sizeof(double), st_));
+          if (!sl.ta_loaded || f == TA_P)
+            CK(cudaMemsetAsync(tacc_ + f * tacc_stride_ + s * kp_.istride, 0, kp_.istride * sizeof(double), st_));
         sl.ta_init = true;
-        sl.ta_total = 0.0;
+        sl.ta_total = sl.ta_loaded ? sl.ta_total_loaded : 0.0;
+        sl.ta_loaded = false;
         sl.ta_dt = 0.0;
       } else {
         w[s] = sl.ta_dt;
@@ -789,6 +799,165 @@ class Solver : public SolverBase {
     CK(cudaStreamSynchronize(st_));
   }
   double tavg_total_time(int id) const override { return slots_[slot_of(id)].ta_total; }
+  double sim_time(int id) const override { return slots_[slot_of(id)].time; }
+
+  // ---------------- checkpoint / restart (io.f90:1173-1267, initial.f90:20-380) ----
+  // The 11 fields of vel.out in record order.
+  static constexpr int kVelFields[11] = {LESGO_U,    LESGO_V,    LESGO_W,    LESGO_RHSX, LESGO_RHSY, LESGO_RHSZ,
+                                         LESGO_CS_OPT2, LESGO_F_LM, LESGO_F_MM, LESGO_F_QN, LESGO_F_NN};
+  // tavg.out's 25 sums in record order (the pressure sum is not written).
+  static constexpr int kTavgFile[25] = {TA_U,   TA_V,   TA_W,   TA_U_W, TA_V_W, TA_W_UV, TA_U2,  TA_V2,  TA_W2,
+                                        TA_UV,  TA_UW,  TA_VW,  TA_TXX, TA_TYY, TA_TZZ,  TA_TXY, TA_TXZ, TA_TYZ,
+                                        TA_FX,  TA_FY,  TA_FZ,  TA_CS,  TA_VORTX, TA_VORTY, TA_VORTZ};
+
+  void checkpoint_write(int id, const std::string& pre, int mpi_names) override {
+    const int slot = slot_of(id);
+    Slot& sl = slots_[slot];
+    const std::string sfx = mpi_names ? ".c0" : "";
+    const long long pl = kp_.plane * d_.nz;
+    std::vector<double> buf(11 * pl);
+    for (int i = 0; i < 11; ++i) get_field(id, kVelFields[i], buf.data() + i * pl, 1, d_.nz);
+    try {
+      {
+        fio::File fl(pre + "vel.out" + sfx, "wb");
+        if (!fl.f) throw fio::IoError{"cannot open " + pre + "vel.out" + sfx};
+        fio::write_record(fl.f, {{buf.data(), (int64_t)buf.size() * 8}});
+      }
+      fio::GridOut go;
+      go.nproc = 1; go.nx = d_.nx; go.ny = d_.ny; go.nz = d_.nz;
+      go.Lx = d_.p.L_x; go.Ly = d_.p.L_y; go.Lz = d_.p.L_z;
+      fio::write_grid(pre + "grid.out", go);
+      if (sl.ta_init) {
+        // sums of x < nx at levels 1..nz, (nx, ny, nz) like the reference
+        fio::File fl(pre + "tavg.out" + sfx, "wb");
+        if (!fl.f) throw fio::IoError{"cannot open " + pre + "tavg.out" + sfx};
+        fio::write_record(fl.f, {{&sl.ta_total, 8}});
+        std::vector<double> lev(pl), pk((size_t)d_.nx * d_.ny * d_.nz);
+        for (int q : kTavgFile) {
+          CK(cudaMemcpyAsync(lev.data(), tacc_ + q * tacc_stride_ + slot * kp_.istride + kp_.plane, pl * sizeof(double),
+                             cudaMemcpyDeviceToHost, st_));
+          CK(cudaStreamSynchronize(st_));
+          for (int k = 0; k < d_.nz; ++k)
+            for (int j = 0; j < d_.ny; ++j)
+              std::memcpy(&pk[((size_t)k * d_.ny + j) * d_.nx], &lev[(size_t)k * kp_.plane + (size_t)j * d_.ld],
+                          d_.nx * sizeof(double));
+          fio::write_record(fl.f, {{pk.data(), (int64_t)pk.size() * 8}});
+        }
+      }
+      // cfl written: the current maximum CFL (fixed time step)
+      double dg[4];
+      diag(id, dg);
+      fio::TimeDat td;
+      td.jt_total = sl.jt_total;
+      td.total_time = sl.time;
+      td.total_time_dim = sl.time * d_.p.z_i / d_.p.u_star;
+      td.dt = d_.p.dt;
+      td.cfl = dg[2];
+      fio::write_time(pre + "total_time.dat", td);
+    } catch (const fio::IoError& e) {
+      throw Error(LESGO_ERR_ARG, "checkpoint: " + e.msg);
+    }
+  }
+
+  // Returns 1 when the checkpoint was of this grid (initu: every field of
+  // vel.out taken, no Euler first step, no Lagrangian initialisation), 0 when
+  // u, v, w were interpolated from another grid (initial.f90:242-380; the
+  // other fields start from zero).
+  int checkpoint_read(int id, const std::string& pre) override {
+    const int slot = slot_of(id);
+    Slot& sl = slots_[slot];
+    const long long pl = kp_.plane * d_.nz;
+    int exact = 0;
+    try {
+      bool interp = false;
+      fio::GridOut g;
+      g.nproc = 1; g.nx = d_.nx; g.ny = d_.ny; g.nz = d_.nz;
+      g.Lx = d_.p.L_x; g.Ly = d_.p.L_y; g.Lz = d_.p.L_z;
+      if (fio::exists(pre + "grid.out")) {
+        g = fio::read_grid(pre + "grid.out");
+        interp = !(g.nproc == 1 && g.nx == d_.nx && g.ny == d_.ny && g.nz == d_.nz && g.Lx == d_.p.L_x &&
+                   g.Ly == d_.p.L_y && g.Lz == d_.p.L_z);
+      }
+      std::vector<char> rec;
+      if (!interp) {
+        std::string name = pre + "vel.out";
+        if (!fio::exists(name)) name += ".c0";
+        fio::File fl(name, "rb");
+        if (!fl.f) throw fio::IoError{"no checkpoint at " + pre + "vel.out"};
+        if (!fio::read_record(fl.f, rec) || (long long)rec.size() != 11 * pl * 8)
+          throw fio::IoError{name + ": record is not 11 fields of (ld, ny, 1:nz)"};
+        for (int i = 0; i < 11; ++i)
+          set_field(id, kVelFields[i], reinterpret_cast<const double*>(rec.data()) + i * pl, 1, d_.nz);
+        exact = 1;
+      } else {
+        if (g.nproc < 1 || g.nx < 2 || g.ny < 1 || g.nz < 2) throw fio::IoError{"grid.out: bad grid"};
+        const int ld_f = 2 * (g.nx / 2 + 1);
+        const int nzt = (g.nz - 1) * g.nproc + 1;
+        const long long pf = (long long)ld_f * g.ny;
+        std::vector<double> uvw[3];
+        for (auto& a : uvw) a.assign((size_t)pf * nzt, 0.0);
+        for (int c = 0; c < g.nproc; ++c) {
+          std::string name = pre + "vel.out" + (g.nproc > 1 ? ".c" + std::to_string(c) : "");
+          if (g.nproc == 1 && !fio::exists(name)) name += ".c0";
+          fio::File fl(name, "rb");
+          if (!fl.f) throw fio::IoError{"cannot open " + name};
+          if (!fio::read_record(fl.f, rec) || (long long)rec.size() < 3 * pf * g.nz * 8)
+            throw fio::IoError{name + ": record shorter than u, v, w of grid.out's grid"};
+          // rank c holds global levels c (nz - 1) + 1 .. c (nz - 1) + nz
+          for (int f = 0; f < 3; ++f)
+            std::memcpy(uvw[f].data() + (size_t)c * (g.nz - 1) * pf,
+                        rec.data() + (size_t)f * pf * g.nz * 8, (size_t)pf * g.nz * 8);
+        }
+        fio::Regrid rg{g.nx, g.ny, nzt, ld_f, g.Lx, g.Ly, g.Lz, d_.nx, d_.ny, d_.nz, d_.ld, d_.dx, d_.dy, d_.dz};
+        std::vector<double> out[3];
+        for (auto& a : out) a.assign((size_t)pl, 0.0);
+        rg.apply(uvw[0].data(), uvw[1].data(), uvw[2].data(), out[0].data(), out[1].data(), out[2].data());
+        std::vector<double> zero((size_t)pl, 0.0);
+        for (int i = 0; i < 11; ++i)
+          set_field(id, kVelFields[i], i < 3 ? out[i].data() : zero.data(), 1, d_.nz);
+      }
+      sl.initu = exact != 0;
+      sl.jt = 0;
+      sl.flm_init = sl.fqn_init = false;
+      if (fio::exists(pre + "total_time.dat")) {
+        const fio::TimeDat t = fio::read_time(pre + "total_time.dat");
+        sl.jt_total = (int)t.jt_total;
+        sl.time = t.total_time;
+      } else {
+        sl.jt_total = 0;
+        sl.time = 0.0;
+      }
+      // time-averaging restart (time_average.f90:114-150)
+      std::string tname = pre + "tavg.out";
+      if (!fio::exists(tname)) tname += ".c0";
+      if (tavg_on_ && fio::exists(tname)) {
+        fio::File fl(tname, "rb");
+        std::vector<char> r;
+        if (!fio::read_record(fl.f, r) || r.size() != 8) throw fio::IoError{tname + ": no total_time record"};
+        std::memcpy(&sl.ta_total_loaded, r.data(), 8);
+        const size_t n3 = (size_t)d_.nx * d_.ny * d_.nz;
+        std::vector<double> lev((size_t)pl, 0.0);
+        for (int q : kTavgFile) {
+          if (!fio::read_record(fl.f, r) || r.size() != n3 * 8) throw fio::IoError{tname + ": bad sum record"};
+          const double* src = reinterpret_cast<const double*>(r.data());
+          for (int k = 0; k < d_.nz; ++k)
+            for (int j = 0; j < d_.ny; ++j)
+              std::memcpy(&lev[(size_t)k * kp_.plane + (size_t)j * d_.ld], src + ((size_t)k * d_.ny + j) * d_.nx,
+                          d_.nx * sizeof(double));
+          CK(cudaMemcpyAsync(tacc_ + q * tacc_stride_ + slot * kp_.istride + kp_.plane, lev.data(),
+                             pl * sizeof(double), cudaMemcpyHostToDevice, st_));
+          CK(cudaStreamSynchronize(st_));
+        }
+        sl.ta_loaded = true;
+        sl.ta_init = false;
+        sl.ta_dt = 0.0;
+        sl.ta_total = 0.0;
+      }
+    } catch (const fio::IoError& e) {
+      throw Error(LESGO_ERR_ARG, "restart: " + e.msg);
+    }
+    return exact;
+  }
 
   int sync() override {
     CK(cudaStreamSynchronize(st_));
@@ -916,6 +1085,10 @@ class Solver : public SolverBase {
     int pending = 0;   // IF_INITLM / IF_INITQN set this step (committed after it)
     bool ta_init = false;          // time averaging started (tavg%init done)
     double ta_dt = 0.0, ta_total = 0.0;
+    bool ta_loaded = false;        // sums read from tavg.out, taken up at the first sample
+    double ta_total_loaded = 0.0;
+    bool initu = false;            // state read from a checkpoint of this grid (initial.f90:77-84)
+    double time = 0.0;             // total_time
   };
 
   int slot_of(int id) const {
@@ -939,16 +1112,16 @@ class Solver : public SolverBase {
   // Per-instance flags of this step (counters already advanced).  Returns
   // true when some flag other than IF_LAG is set (a step that is not replayed).
   bool upload_flags(bool count_euler, bool* lag_any) {
-    const bool inilag = !d_.p.initu;
     std::vector<int> fl(slots_.size(), 0);
     bool special = false, lag = false;
     for (size_t s = 0; s < slots_.size(); ++s) {
       Slot& sl = slots_[s];
+      const bool inilag = !sl.initu;
       int f = 0;
-      if (count_euler && sl.jt_total == 1 && !d_.p.initu) f |= IF_EULER;
+      if (count_euler && sl.jt_total == 1 && !sl.initu) f |= IF_EULER;
       const bool cs_fill = (sl.jt == 1 && inilag);
       if (cs_fill) f |= IF_CSFILL;
-      if (!cs_fill && (sl.jt >= d_.p.dyn_init || d_.p.initu) && (sl.jt_total % d_.p.cs_count == 0)) {
+      if (!cs_fill && (sl.jt >= d_.p.dyn_init || sl.initu) && (sl.jt_total % d_.p.cs_count == 0)) {
         f |= IF_LAG;
         if (inilag && !sl.flm_init && (sl.jt == d_.p.cs_count || sl.jt == d_.p.dyn_init)) f |= IF_INITLM;
         if (inilag && !sl.fqn_init && (sl.jt == d_.p.cs_count || sl.jt == d_.p.dyn_init)) f |= IF_INITQN;
@@ -1971,3 +2144,58 @@ int lesgo_gpu_tavg_total_time(lesgo_handle_t* h, int id, double* t) {
   return guarded(h, [&] { *t = h->s->tavg_total_time(id < 0 ? h->inst0 : id); });
 }
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Checkpoint / restart files
+// ---------------------------------------------------------------------------
+extern "C" {
+int lesgo_gpu_checkpoint_write(lesgo_handle_t* h, const char* path, int mpi_names) {
+  if (!path) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->checkpoint_write(h->inst0, path, mpi_names); });
+}
+int lesgo_gpu_checkpoint_write_inst(lesgo_handle_t* h, int id, const char* path, int mpi_names) {
+  if (!path) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->checkpoint_write(id, path, mpi_names); });
+}
+int lesgo_gpu_checkpoint_read(lesgo_handle_t* h, const char* path, int* same_grid) {
+  if (!path) return LESGO_ERR_ARG;
+  return guarded(h, [&] {
+    const int e = h->s->checkpoint_read(h->inst0, path);
+    if (same_grid) *same_grid = e;
+  });
+}
+int lesgo_gpu_checkpoint_read_inst(lesgo_handle_t* h, int id, const char* path, int* same_grid) {
+  if (!path) return LESGO_ERR_ARG;
+  return guarded(h, [&] {
+    const int e = h->s->checkpoint_read(id, path);
+    if (same_grid) *same_grid = e;
+  });
+}
+int lesgo_gpu_sim_time(lesgo_handle_t* h, int id, double* total_time) {
+  if (!total_time) return LESGO_ERR_ARG;
+  return guarded(h, [&] { *total_time = h->s->sim_time(id < 0 ? h->inst0 : id); });
+}
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// lesgo.conf
+// ---------------------------------------------------------------------------
+extern "C" int lesgo_gpu_read_conf(const char* path, int with_turbines, lesgo_params_t* p, lesgo_run_t* run,
+                                   lesgo_turbine_t* turbines, int max_turbines, char* log, int loglen) {
+  if (!path || !p || !run || (with_turbines && max_turbines > 0 && !turbines)) return LESGO_ERR_ARG;
+  try {
+    std::string lg;
+    lesgo::conf::read(path, with_turbines, p, run, turbines, with_turbines ? max_turbines : 0, &lg);
+    if (log && loglen > 0) {
+      std::strncpy(log, lg.c_str(), (size_t)loglen - 1);
+      log[loglen - 1] = '\0';
+    }
+    return LESGO_OK;
+  } catch (const lesgo::conf::ConfError& e) {
+    g_create_err = e.msg;
+    return e.code;
+  } catch (const std::exception& e) {
+    g_create_err = e.what();
+    return LESGO_ERR_ARG;
+  }
+}

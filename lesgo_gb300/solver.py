@@ -14,6 +14,7 @@ reference would print and ``stop`` (messages.f90:228-239).
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Dict, Iterable, Optional
 
 import numpy as np
@@ -71,6 +72,31 @@ def make_turbines(turbines):
         for k in ("xloc", "yloc", "height", "dia", "thk", "theta1", "theta2", "Ct_prime"):
             setattr(arr[i], k, float(t.get(k, 1.33 if k == "Ct_prime" else 0.0)))
     return arr, len(tl)
+
+
+def read_conf(path: str, with_turbines: bool = True, max_turbines: int = 4096):
+    """<path>lesgo.conf -> (parameter keywords for LesgoGPU / make_params, run
+    control dict, notes on unused blocks and keys).  `path` is a prefix like
+    the reference's `path` ("" or a directory with its trailing '/')."""
+    lib = L.load()
+    p, run = L.Params(), L.Run()
+    tb = (L.Turbine * max(1, max_turbines))()
+    log = C.create_string_buffer(1 << 14)
+    rc = lib.lesgo_gpu_read_conf(os.fsencode(path), 1 if with_turbines else 0, C.byref(p), C.byref(run),
+                                 C.cast(tb, C.POINTER(L.Turbine)), max_turbines, log, len(log))
+    if rc != L.LESGO_OK:
+        raise LesgoError(rc, lib.lesgo_gpu_last_error(None).decode())
+    kw = dict(nx=p.nx, ny=p.ny, Nz=p.nz_tot)
+    for name in ("L_x", "L_y", "L_z", "z_i", "u_star", "vonk", "zo", "dt", "nu_molec", "ubot", "utop",
+                 "mean_p_force_x", "mean_p_force_y", "alpha1", "alpha2", "filter_cutoff", "T_avg_dim"):
+        kw[name] = getattr(p, name)
+    for name in ("sgs_model", "cs_count", "dyn_init", "ifilter", "lbc_mom", "ubc_mom"):
+        kw[name] = getattr(p, name)
+    for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction"):
+        kw[name] = bool(getattr(p, name))
+    kw["turbines"] = [{k: getattr(tb[i], k) for k, _ in L.Turbine._fields_} for i in range(p.n_turbines)]
+    rd = {k: getattr(run, k) for k, _ in L.Run._fields_}
+    return kw, rd, log.value.decode()
 
 
 def footprint_bytes(capacity: int = 1, **kw) -> int:
@@ -303,6 +329,22 @@ class LesgoGPU:
                                                      out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
         return out
 
+    # ---------------- checkpoint / restart ---------------------------------------------
+    def checkpoint_write(self, path: str, mpi_names: bool = False):
+        """vel.out, grid.out, total_time.dat (and tavg.out) under the prefix `path`."""
+        self._check(self._lib.lesgo_gpu_checkpoint_write(self._h, os.fsencode(path), 1 if mpi_names else 0))
+
+    def checkpoint_read(self, path: str) -> bool:
+        """Restart from the files under `path`; True when they were of this grid."""
+        same = C.c_int()
+        self._check(self._lib.lesgo_gpu_checkpoint_read(self._h, os.fsencode(path), C.byref(same)))
+        return bool(same.value)
+
+    def sim_time(self) -> float:
+        t = C.c_double()
+        self._check(self._lib.lesgo_gpu_sim_time(self._h, -1, C.byref(t)))
+        return t.value
+
     def tavg_total_time(self) -> float:
         t = C.c_double()
         self._check(self._lib.lesgo_gpu_tavg_total_time(self._h, -1, C.byref(t)))
@@ -433,6 +475,22 @@ class LesgoBatch:
         self._check(self._lib.lesgo_gpu_tavg_profile_inst(self._h, iid, TAVG_QUANTITIES.index(name),
                                                      out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
         return out
+
+    # ---------------- checkpoint / restart ---------------------------------------------
+    def checkpoint_write(self, iid: int, path: str, mpi_names: bool = False):
+        """vel.out, grid.out, total_time.dat (and tavg.out) under the prefix `path`."""
+        self._check(self._lib.lesgo_gpu_checkpoint_write_inst(self._h, iid, os.fsencode(path), 1 if mpi_names else 0))
+
+    def checkpoint_read(self, iid: int, path: str) -> bool:
+        """Restart from the files under `path`; True when they were of this grid."""
+        same = C.c_int()
+        self._check(self._lib.lesgo_gpu_checkpoint_read_inst(self._h, iid, os.fsencode(path), C.byref(same)))
+        return bool(same.value)
+
+    def sim_time(self, iid: int) -> float:
+        t = C.c_double()
+        self._check(self._lib.lesgo_gpu_sim_time(self._h, iid, C.byref(t)))
+        return t.value
 
     def tavg_total_time(self, iid: int) -> float:
         t = C.c_double()

@@ -30,6 +30,7 @@ Conventions
 from __future__ import annotations
 
 import math
+import struct
 from dataclasses import dataclass, field
 from typing import List, Optional
 
@@ -268,6 +269,7 @@ class Oracle:
         self.ustar_lbc = np.zeros((ny, p.nx))
         self.jt = 0
         self.jt_total = 0
+        self.time = 0.0
         self.F_LM_MM_init = False
         self.F_QN_NN_init = False
         self._init_wavenumber()
@@ -1153,6 +1155,7 @@ class Oracle:
         """main.f90:143-157."""
         self.jt_total += 1
         self.jt += 1
+        self.time += self.p.dt
         self.RHSx_f[:] = self.RHSx
         self.RHSy_f[:] = self.RHSy
         self.RHSz_f[:] = self.RHSz
@@ -1271,9 +1274,16 @@ class TimeAverage:
                     self.compute()
 
     def init(self):
+        """time_average.f90:63-173: zero sums, or the sums of tavg.out."""
         for a in self.acc.values():
             a[:] = 0.0
         self.total_time = 0.0
+        if getattr(self, "loaded", None) is not None:
+            total, sums = self.loaded
+            for n, a in sums.items():
+                self.acc[n][:] = a
+            self.total_time = total
+            self.loaded = None
         self.dt = 0.0
         self.initialized = True
 
@@ -1335,6 +1345,221 @@ class TimeAverage:
             a, b, c = rs[name]
             return A(a) - A(b) * A(c)
         return A(name)
+
+
+# ---------------------------------------------------------------------------
+# Restart files: io.f90:1173-1267 (checkpoint), initial.f90:20-380 (restart,
+# ic_interp), io.f90:60-96 (total_time.dat), time_average.f90:114-150 and
+# :665-716 (tavg.out).  Fortran sequential unformatted records as gfortran
+# frames them: 4-byte little-endian length before and after the payload; a
+# payload above SUBMAX bytes is split into subrecords, the leading length
+# negated when more follow, the trailing length negated when one precedes.
+# ---------------------------------------------------------------------------
+SUBMAX = 2147483639
+VEL_FIELDS = ["u", "v", "w", "RHSx", "RHSy", "RHSz", "Cs_opt2", "F_LM", "F_MM", "F_QN", "F_NN"]
+TAVG_FILE = [n for n in TAVG_NAMES if n != "p"]
+
+
+def fortran_record_bytes(payload: bytes, submax: int = SUBMAX) -> bytes:
+    out = bytearray()
+    left, off, first = len(payload), 0, True
+    while True:
+        n = min(left, submax)
+        more = left > n
+        out += struct.pack("<i", -n if more else n)
+        out += payload[off:off + n]
+        out += struct.pack("<i", n if first else -n)
+        off += n
+        left -= n
+        first = False
+        if left <= 0:
+            return bytes(out)
+
+
+def fortran_records(data: bytes):
+    """Split a file's bytes into record payloads."""
+    recs, pos = [], 0
+    while pos < len(data):
+        buf, first = bytearray(), True
+        while True:
+            lead, = struct.unpack_from("<i", data, pos)
+            n = abs(lead)
+            buf += data[pos + 4:pos + 4 + n]
+            trail, = struct.unpack_from("<i", data, pos + 4 + n)
+            if abs(trail) != n or (trail < 0) == first:
+                raise ValueError("bad record marker")
+            pos += 8 + n
+            first = False
+            if lead >= 0:
+                break
+        recs.append(bytes(buf))
+    return recs
+
+
+def write_checkpoint(o: "Oracle", prefix: str, ta: Optional["TimeAverage"] = None, mpi_names: bool = False):
+    p = o.p
+    sfx = ".c0" if mpi_names else ""
+    payload = b"".join(np.ascontiguousarray(oracle_state(o, n)[1:p.nz + 1]).tobytes() for n in VEL_FIELDS)
+    with open(prefix + "vel.out" + sfx, "wb") as f:
+        f.write(fortran_record_bytes(payload))
+    with open(prefix + "grid.out", "wb") as f:
+        f.write(fortran_record_bytes(struct.pack("<4i3d", 1, p.nx, p.ny, p.nz, p.L_x, p.L_y, p.L_z)))
+    if ta is not None and ta.initialized:
+        with open(prefix + "tavg.out" + sfx, "wb") as f:
+            f.write(fortran_record_bytes(struct.pack("<d", ta.total_time)))
+            for n in TAVG_FILE:
+                f.write(fortran_record_bytes(np.ascontiguousarray(ta.acc[n][1:]).tobytes()))
+    with open(prefix + "total_time.dat", "w") as f:
+        f.write(" %d %.17E %.17E %.17E %.17E\n" % (o.jt_total, o.time, o.time * p.z_i / p.u_star, p.dt,
+                                                  o.max_cfl()))
+
+
+def oracle_state(o: "Oracle", name: str) -> np.ndarray:
+    return o.pres if name == "p" else getattr(o, name)
+
+
+def binary_search(arr, val) -> int:
+    """functions.f90:811-860 (1-based interval index, 0 below, N above)."""
+    n = len(arr)
+    if val < arr[0]:
+        return 0
+    if val > arr[n - 1]:
+        return n
+    low, high = 1, n
+    while high - low > 1:
+        mid = (low + high) // 2
+        if arr[mid - 1] > val:
+            high = mid
+        elif arr[mid - 1] < val:
+            low = mid
+        else:
+            return mid
+    return low
+
+
+def ic_interp(p: Params, grid_f, uf, vf, wf):
+    """initial.f90:242-380: u, v, w (levels 1..nz_f of the file grid, arrays
+    (nz_f, ny_f, ld_f)) onto the grid of p, arrays (nz, ny, ld) at levels 1..nz."""
+    nx_f, ny_f, nz_f, Lx_f, Ly_f, Lz_f = grid_f
+    dx_f, dy_f, dz_f = Lx_f / nx_f, Ly_f / ny_f, Lz_f / (nz_f - 1)
+    x_f = [i * Lx_f / nx_f for i in range(nx_f)]
+    y_f = [j * Ly_f / ny_f for j in range(ny_f)]
+    zw_r = [k * dz_f for k in range(nz_f)]
+    z_r = [z + 0.5 * dz_f for z in zw_r]
+    out = [np.zeros((p.nz, p.ny, p.ld)) for _ in range(3)]
+
+    def F(a, i, j, k):
+        return a[k - 1, j - 1, i - 1]
+
+    for i in range(1, p.nx + 1):
+        xg = (i - 1) * p.dx
+        xx = xg - math.floor(xg / Lx_f) * Lx_f
+        i1 = binary_search(x_f, xx)
+        i2 = i1 % nx_f + 1
+        bx = (xx - x_f[i1 - 1]) / dx_f
+        ax = 1.0 - bx
+        for j in range(1, p.ny + 1):
+            yg = (j - 1) * p.dy
+            yy = yg - math.floor(yg / Ly_f) * Ly_f
+            j1 = binary_search(y_f, yy)
+            j2 = j1 % ny_f + 1
+            by = (yy - y_f[j1 - 1]) / dy_f
+            ay = 1.0 - by
+
+            def plane(a, kk):
+                return (ax * ay * F(a, i1, j1, kk) + bx * ay * F(a, i2, j1, kk) + ax * by * F(a, i1, j2, kk)
+                        + bx * by * F(a, i2, j2, kk))
+
+            def vol(a, k1, az, bz):
+                return (ax * ay * az * F(a, i1, j1, k1) + bx * ay * az * F(a, i2, j1, k1)
+                        + ax * by * az * F(a, i1, j2, k1) + bx * by * az * F(a, i2, j2, k1)
+                        + ax * ay * bz * F(a, i1, j1, k1 + 1) + bx * ay * bz * F(a, i2, j1, k1 + 1)
+                        + ax * by * bz * F(a, i1, j2, k1 + 1) + bx * by * bz * F(a, i2, j2, k1 + 1))
+
+            for k in range(1, p.nz + 1):
+                z = (k - 0.5) * p.dz
+                k1 = binary_search(z_r, z)
+                for a, o in ((uf, out[0]), (vf, out[1])):
+                    if k1 == nz_f:
+                        o[k - 1, j - 1, i - 1] = plane(a, k1)
+                    elif k1 == 0:
+                        o[k - 1, j - 1, i - 1] = plane(a, 1)
+                    else:
+                        bz = (z - z_r[k1 - 1]) / dz_f
+                        o[k - 1, j - 1, i - 1] = vol(a, k1, 1.0 - bz, bz)
+                zw = (k - 1) * p.dz
+                k1 = binary_search(zw_r, zw)
+                if k1 == nz_f:
+                    out[2][k - 1, j - 1, i - 1] = plane(wf, k1)
+                elif k1 == 0:
+                    out[2][k - 1, j - 1, i - 1] = plane(wf, 1)
+                else:
+                    bz = (zw - zw_r[k1 - 1]) / dz_f
+                    out[2][k - 1, j - 1, i - 1] = vol(wf, k1, 1.0 - bz, bz)
+    return out
+
+
+def read_checkpoint(o: "Oracle", prefix: str, ta: Optional["TimeAverage"] = None) -> bool:
+    """Restart o from the files under prefix (initial.f90:20-239, io.f90:60-96);
+    True when the checkpoint was of this grid (initu)."""
+    import os
+    p = o.p
+    nproc, nx_f, ny_f, nz_f, Lx_f, Ly_f, Lz_f = 1, p.nx, p.ny, p.nz, p.L_x, p.L_y, p.L_z
+    if os.path.exists(prefix + "grid.out"):
+        with open(prefix + "grid.out", "rb") as f:
+            rec, = fortran_records(f.read())
+        nproc, nx_f, ny_f, nz_f, Lx_f, Ly_f, Lz_f = struct.unpack("<4i3d", rec)
+    exact = (nproc == 1 and nx_f == p.nx and ny_f == p.ny and nz_f == p.nz and Lx_f == p.L_x
+             and Ly_f == p.L_y and Lz_f == p.L_z)
+    shape = (p.nz, p.ny, p.ld)
+    if exact:
+        name = prefix + "vel.out"
+        if not os.path.exists(name):
+            name += ".c0"
+        with open(name, "rb") as f:
+            rec = fortran_records(f.read())[0]
+        a = np.frombuffer(rec, dtype="<f8").reshape((11,) + shape)
+        for n, arr in zip(VEL_FIELDS, a):
+            oracle_state(o, n)[1:] = arr
+    else:
+        ld_f = 2 * (nx_f // 2 + 1)
+        nzt = (nz_f - 1) * nproc + 1
+        g = [np.zeros((nzt, ny_f, ld_f)) for _ in range(3)]
+        for c in range(nproc):
+            name = prefix + "vel.out" + (".c%d" % c if nproc > 1 else "")
+            if nproc == 1 and not os.path.exists(name):
+                name += ".c0"
+            with open(name, "rb") as f:
+                rec = fortran_records(f.read())[0]
+            blk = np.frombuffer(rec[:3 * nz_f * ny_f * ld_f * 8], dtype="<f8").reshape(3, nz_f, ny_f, ld_f)
+            for fi in range(3):
+                g[fi][c * (nz_f - 1):c * (nz_f - 1) + nz_f] = blk[fi]
+        u, v, w = ic_interp(p, (nx_f, ny_f, nzt, Lx_f, Ly_f, Lz_f), *g)
+        for n in VEL_FIELDS:
+            oracle_state(o, n)[1:] = 0.0
+        o.u[1:], o.v[1:], o.w[1:] = u, v, w
+    p.initu = exact
+    o.jt = 0
+    o.F_LM_MM_init = o.F_QN_NN_init = False
+    o.jt_total, o.time = 0, 0.0
+    if os.path.exists(prefix + "total_time.dat"):
+        with open(prefix + "total_time.dat") as f:
+            vals = f.read().replace(",", " ").replace("D", "E").split()
+        o.jt_total, o.time = int(vals[0]), float(vals[1])
+    tname = prefix + "tavg.out"
+    if not os.path.exists(tname):
+        tname += ".c0"
+    if ta is not None and os.path.exists(tname):
+        with open(tname, "rb") as f:
+            recs = fortran_records(f.read())
+        total, = struct.unpack("<d", recs[0])
+        sums = {n: np.zeros((p.nz + 1, p.ny, p.nx)) for n in TAVG_FILE}
+        for n, r in zip(TAVG_FILE, recs[1:]):
+            sums[n][1:] = np.frombuffer(r, dtype="<f8").reshape(p.nz, p.ny, p.nx)
+        ta.loaded = (total, sums)
+        ta.initialized = False
+        ta.dt = 0.0
+    return exact
 
 
 def tridag_array(a, b, c, r, mask):

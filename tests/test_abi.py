@@ -55,6 +55,21 @@ def test_params_layout_matches_c(tmp_path):
         assert getattr(_lib.Params, f).offset == off, f
 
 
+def test_run_layout_matches_c(tmp_path):
+    from lesgo_gb300 import _lib
+    src = tmp_path / "run.c"
+    fields = [f[0] for f in _lib.Run._fields_]
+    body = "\n".join(f'printf("%zu\\n", offsetof(lesgo_run_t, {f}));' for f in fields)
+    src.write_text(f'#include <stdio.h>\n#include <stddef.h>\n#include "lesgo_gpu.h"\n'
+                   f'int main(void){{printf("%zu\\n", sizeof(lesgo_run_t));\n{body}\nreturn 0;}}\n')
+    exe = tmp_path / "run"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals[0] == C.sizeof(_lib.Run)
+    for f, off in zip(fields, vals[1:]):
+        assert getattr(_lib.Run, f).offset == off, f
+
+
 def test_params_default_on_host(built_lib):
     from lesgo_gb300 import _lib
     lib = _lib.load()
