@@ -95,6 +95,10 @@ typedef struct {
   const lesgo_turbine_t* turbines;
   double alpha1, alpha2, filter_cutoff, T_avg_dim;
   int adm_correction;
+  /* time step chosen every step from the CFL number (cfl_util.f90:70-111,
+   * main.f90:135-144); dt is then the step before the first one */
+  int use_cfl_dt;
+  double cfl;
 } lesgo_params_t;
 
 /* The run-control values of lesgo.conf that lesgo_params_t does not carry
@@ -306,6 +310,9 @@ int lesgo_gpu_checkpoint_read(lesgo_handle_t* h, const char* path, int* same_gri
 int lesgo_gpu_checkpoint_read_inst(lesgo_handle_t* h, int id, const char* path, int* same_grid);
 /* total_time of instance id (id < 0: the handle's single instance). */
 int lesgo_gpu_sim_time(lesgo_handle_t* h, int id, double* total_time);
+/* dt of instance id's last step (with use_cfl_dt the one cfl_util.f90:70-111
+ * chose on the device; before the first step the input dt). */
+int lesgo_gpu_time_step(lesgo_handle_t* h, int id, double* dt);
 
 /* ---- instrumentation (no reference counterpart; the reference only
  * prints wall-clock times, main.f90:359-436) --------------------------- */

@@ -48,6 +48,7 @@ class Params(C.Structure):
         ("turbines", C.POINTER(Turbine)),
         ("alpha1", C.c_double), ("alpha2", C.c_double), ("filter_cutoff", C.c_double), ("T_avg_dim", C.c_double),
         ("adm_correction", C.c_int),
+        ("use_cfl_dt", C.c_int), ("cfl", C.c_double),
     ]
 
 
@@ -126,6 +127,7 @@ SIGNATURES = {
     "lesgo_gpu_checkpoint_read": (_I, [_H, C.c_char_p, C.POINTER(_I)]),
     "lesgo_gpu_checkpoint_read_inst": (_I, [_H, _I, C.c_char_p, C.POINTER(_I)]),
     "lesgo_gpu_sim_time": (_I, [_H, _I, _D]),
+    "lesgo_gpu_time_step": (_I, [_H, _I, _D]),
     "lesgo_gpu_read_conf": (_I, [C.c_char_p, _I, C.POINTER(Params), C.POINTER(Run), C.POINTER(Turbine), _I,
                                  C.c_char_p, _I]),
     "lesgo_gpu_profile": (_I, [_H, _I]),

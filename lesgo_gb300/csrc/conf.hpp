@@ -100,7 +100,8 @@ static void defaults(lesgo_params_t* p, lesgo_run_t* r) {
   p->n_turbines = 0; p->turbines = nullptr;
   r->nproc = 1; r->uniform_spacing = 0; r->wall_damp_exp = 2; r->Co = 0.16; r->sgs = 1;
   r->nsteps = 50000; r->runtime = -1; r->use_cfl_dt = 0;
-  r->cfl = (double)0.05f;   // param.f90: a default-real literal
+  r->cfl = p->cfl = (double)0.05f;   // param.f90: a default-real literal
+  p->use_cfl_dt = 0;
   r->cumulative_time = 1; r->inilag = 1;
   r->wbase = 100; r->nenergy = 100; r->lag_cfl_count = 1000;
   r->checkpoint_data = 0; r->checkpoint_nskip = 10000;
@@ -292,8 +293,8 @@ static void read(const std::string& path, int with_turbines, lesgo_params_t* p, 
       } else if (block == "TIME") {
         if (key == "NSTEPS") r->nsteps = rd.as_int(v);
         else if (key == "RUNTIME") r->runtime = rd.as_int(v);
-        else if (key == "USE_CFL_DT") r->use_cfl_dt = rd.as_bool(v);
-        else if (key == "CFL") r->cfl = rd.as_real(v);
+        else if (key == "USE_CFL_DT") r->use_cfl_dt = p->use_cfl_dt = rd.as_bool(v);
+        else if (key == "CFL") r->cfl = p->cfl = rd.as_real(v);
         else if (key == "DT") p->dt = rd.as_real(v);
         else if (key == "CUMULATIVE_TIME") r->cumulative_time = rd.as_bool(v);
         else used = false;

@@ -310,7 +310,7 @@ __global__ void k_interp(InterpArgs<R> a) {
   const long long q = x_.q;
   const long long ib = x_.inst * kp.istride;
   const int nz = kp.nz;
-  const double ldt = kp.lagran_dt, dz = kp.dz;
+  const double ldt = kp.sc[x_.inst * SC_N + SC_LDT], dz = kp.dz;
   const double x = i * kp.dx, y = j * kp.dy;
   auto zc = [&](int kk) { return (kk - 0.5) * dz; };          // grid%z
   auto zwc = [&](int kk) { return zc(kk) - dz / 2.0; };       // grid%zw
@@ -548,7 +548,8 @@ __global__ void k_wproj(const R* __restrict__ p, R* dpdz, R* RHSz, R* u, R* v, R
   if (!FUSED) { dpdz[q] = d; return; }
   RHSz[q] = RHSz[q] - d;
   const int nz = kp.nz;
-  if (k >= 2 && k <= nz - 1) w[q] = w[q] + (R)kp.dt * (-(R)kp.tadv1 * d);
+  const double* c = kp.sc + x.inst * SC_N;
+  if (k >= 2 && k <= nz - 1) w[q] = w[q] + (R)c[SC_DT] * (-(R)c[SC_T1] * d);
   if (k == 1) w[q] = (R)0;
   if (k == nz) {
     w[q] = (R)0;
@@ -565,7 +566,8 @@ __global__ void k_project(const R* dpdx, const R* dpdy, const R* dpdz, R* u, R* 
   const PtIdx x = pt_index(t, kp);
   const int k = x.k;
   const long long q = x.q;
-  const R dt = (R)kp.dt, t1 = (R)kp.tadv1;
+  const double* c = kp.sc + x.inst * SC_N;
+  const R dt = (R)c[SC_DT], t1 = (R)c[SC_T1];
   if (k <= kp.nz - 1) {
     u[q] = u[q] + dt * (-t1 * dpdx[q]);
     v[q] = v[q] + dt * (-t1 * dpdy[q]);
@@ -617,7 +619,8 @@ __global__ void k_ab2(R* u, R* v, R* w, const R* RHSx, const R* RHSy, const R* R
   const long long t = gt % n;
   const long long q = (gt / n) * kp.istride + pl + t;
   const int k = 1 + (int)(t / pl);
-  const R dt = (R)kp.dt, t1 = (R)kp.tadv1, t2 = (R)kp.tadv2;
+  const double* c = kp.sc + (gt / n) * SC_N;
+  const R dt = (R)c[SC_DT], t1 = (R)c[SC_T1], t2 = (R)c[SC_T2];
   if (k <= kp.nz - 1) {
     u[q] = u[q] + dt * (t1 * RHSx[q] + t2 * fx[q]);
     v[q] = v[q] + dt * (t1 * RHSy[q] + t2 * fy[q]);
@@ -761,7 +764,9 @@ struct TurbDev {
   double* u_d_T;
   double* f_n;
   double* disk;             // scratch per turbine
-  double eps, dvol;
+  const int* tinst;         // instance of each turbine
+  const double* sc;         // step constants (disk-velocity filter weight)
+  double dvol;
   const double* dia;
 };
 
@@ -788,7 +793,8 @@ __global__ void __launch_bounds__(256) k_turb_disk(TurbDev td, const R* u, const
   if (threadIdx.x == 0) {
     double ud = sh[0];
     ud = ud / td.corr[s];
-    const double udT = (1.0 - td.eps) * td.u_d_T[s] + td.eps * ud;
+    const double eps = td.sc[td.tinst[s] * SC_N + SC_EPS];
+    const double udT = (1.0 - eps) * td.u_d_T[s] + eps * ud;
     td.u_d[s] = ud;
     td.u_d_T[s] = udT;
     // turbines.f90:583: -0.5*Ct'*abs(u_d_T)*u_d_T*0.25*pi*dia**2
@@ -962,6 +968,105 @@ __global__ void k_plane_mean(const double* f, int nx, int ny, int ld, double* ou
     __syncthreads();
   }
   if (threadIdx.x == 0) out[blockIdx.x] = sh[0] / ((double)nx * ny);
+}
+
+}  // namespace lesgo
+
+namespace lesgo {
+
+// ---------------------------------------------------------------------------
+// Time step on the device.  k_cfl_max: per instance the maxima of |u|, |v|,
+// |w| over x < nx and levels 1..nz-1 (cfl_util.f90:70-111), folded into
+// mx[inst][3] as the bit patterns of non-negative doubles (ordered like the
+// values).  Grid (blocks, instances).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) k_cfl_max(const R* u, const R* v, const R* w, KP kp,
+                                                 unsigned long long* mx) {
+  __shared__ double sh[3][256];
+  const int inst = blockIdx.y;
+  const long long m = (long long)kp.nx * kp.ny * (kp.nz - 1);
+  const long long base = inst * kp.istride + kp.plane;
+  double au = 0.0, av = 0.0, aw = 0.0;
+  for (long long t = blockIdx.x * 256LL + threadIdx.x; t < m; t += (long long)gridDim.x * 256) {
+    const int i = (int)(t % kp.nx);
+    const long long r = t / kp.nx;
+    const int j = (int)(r % kp.ny);
+    const long long k = r / kp.ny;   // 0 .. nz-2 (level k + 1)
+    const long long q = base + k * kp.plane + (long long)j * kp.ld + i;
+    au = fmax(au, fabs((double)u[q]));
+    av = fmax(av, fabs((double)v[q]));
+    aw = fmax(aw, fabs((double)w[q]));
+  }
+  sh[0][threadIdx.x] = au; sh[1][threadIdx.x] = av; sh[2][threadIdx.x] = aw;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] = fmax(sh[c][threadIdx.x], sh[c][threadIdx.x + st]);
+    __syncthreads();
+  }
+  if (threadIdx.x < 3)
+    atomicMax(&mx[inst * 3 + threadIdx.x], (unsigned long long)__double_as_longlong(sh[threadIdx.x][0]));
+}
+
+// Start of a step, one thread per instance: with cfl_mode, dt from the maxima
+// (cfl_util.f90:70-111) and the AB2 weights for a varying step (main.f90:
+// 135-144), the pressure-RHS scale, the disk filter weight, lagran_dt
+// (sgs_stag_util.f90:72-83, reset lagrange_Sdep.f90:430); always total_time
+// and the pending time-average weight (io.f90:559-562).
+struct StepBeginArgs {
+  double* sc;
+  const int* iflags;
+  unsigned long long* mx;
+  int ninst, cfl_mode;
+  double cfl, dx, dy, dz, c1, z_i, u_star, T_avg_dim;
+};
+
+__global__ void k_step_begin(StepBeginArgs a) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= a.ninst) return;
+  double* c = a.sc + inst * SC_N;
+  const int f = a.iflags[inst];
+  if (a.cfl_mode) {
+    const double iu = __longlong_as_double((long long)a.mx[inst * 3 + 0]) / a.dx;
+    const double iv = __longlong_as_double((long long)a.mx[inst * 3 + 1]) / a.dy;
+    const double iw = __longlong_as_double((long long)a.mx[inst * 3 + 2]) / a.dz;
+    a.mx[inst * 3 + 0] = 0ULL; a.mx[inst * 3 + 1] = 0ULL; a.mx[inst * 3 + 2] = 0ULL;
+    double m = iu;
+    if (iv > m) m = iv;
+    if (iw > m) m = iw;
+    const double dt_f = c[SC_DT];
+    const double dt = a.cfl / m;
+    c[SC_DTF] = dt_f;
+    c[SC_DT] = dt;
+    c[SC_T1] = 1.0 + 0.5 * dt / dt_f;
+    c[SC_T2] = 1.0 - c[SC_T1];
+    c[SC_PS] = a.c1 / c[SC_T1] / dt;
+    if (a.T_avg_dim > 0) {
+      const double dt_dim = dt * a.z_i / a.u_star;
+      c[SC_EPS] = (dt_dim / a.T_avg_dim) / (1. + dt_dim / a.T_avg_dim);
+    }
+    if (f & IF_LAGRESET) c[SC_LDT] = 0.0;
+    if (f & IF_LAGACC) c[SC_LDT] = c[SC_LDT] + dt;
+  }
+  c[SC_TIME] = c[SC_TIME] + c[SC_DT];
+  if (f & IF_TAACC) c[SC_TAW] = c[SC_TAW] + c[SC_DT];
+}
+
+// Time-averaging bookkeeping after a step, one thread per instance: act 1
+// starts fresh sums (tavg%init), 2 starts from sums read from tavg.out, 3
+// takes a sample weighted by the pending time (tavg%compute); w receives the
+// sample weight (0: none).
+__global__ void k_tavg_prep(double* sc, const int* act, double* w, int ninst) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= ninst) return;
+  double* c = sc + inst * SC_N;
+  const int a = act[inst];
+  double wt = 0.0;
+  if (a == 1) { c[SC_TAW] = 0.0; c[SC_TAT] = 0.0; }
+  else if (a == 2) { c[SC_TAW] = 0.0; }
+  else if (a == 3) { wt = c[SC_TAW]; c[SC_TAT] = c[SC_TAT] + wt; c[SC_TAW] = 0.0; }
+  w[inst] = wt;
 }
 
 }  // namespace lesgo

@@ -74,6 +74,7 @@ struct Derived {
     if (p.cs_count < 1) throw Error(LESGO_ERR_ARG, "cs_count must be >= 1");
     if (p.precision != LESGO_FP64 && p.precision != LESGO_MIXED) throw Error(LESGO_ERR_ARG, "precision");
     if (p.dt <= 0 || p.L_x <= 0 || p.L_y <= 0 || p.L_z <= 0 || p.zo <= 0) throw Error(LESGO_ERR_ARG, "non-positive length/time");
+    if (p.use_cfl_dt && !(p.cfl > 0)) throw Error(LESGO_ERR_ARG, "use_cfl_dt needs cfl > 0");
     nx = p.nx; ny = p.ny;
     const int nproc = 1;
     nz = p.nz_tot / nproc + 1;
@@ -206,6 +207,7 @@ struct TurbineHost {
   std::vector<double> win_ind;
   std::vector<long long> cols;    // (jy*ld + i) of footprint columns
   std::vector<double> nhat, ctp, corr, dia;
+  std::vector<int> tinst;         // instance (slot) of each turbine
 };
 
 // Node lists of the actuator disks of every active instance, with absolute
@@ -276,6 +278,7 @@ static TurbineHost turbines_build(const Derived& d, const std::vector<std::vecto
       th.corr.push_back(P.adm_correction ? (1 + 0.25 * (1 - ind.M) * t.Ct_prime) : 1.0);
       th.dia.push_back(t.dia);
       inst_of.push_back((int)inst);
+      th.tinst.push_back((int)inst);
       ++th.n;
     }
   }
@@ -352,10 +355,11 @@ class SolverBase {
   virtual void tavg_sample() = 0;
   virtual void tavg_get(int id, int which, double* host, int lbz, int nzhi) = 0;
   virtual void tavg_profile(int id, int which, double* prof, int n) = 0;
-  virtual double tavg_total_time(int id) const = 0;
+  virtual double tavg_total_time(int id) = 0;
   virtual void checkpoint_write(int id, const std::string& path, int mpi_names) = 0;
   virtual int checkpoint_read(int id, const std::string& path) = 0;
-  virtual double sim_time(int id) const = 0;
+  virtual double sim_time(int id) = 0;
+  virtual double time_step(int id) = 0;
 };
 
 // Device bytes of a handle (the admission footprint of a batch).
@@ -387,9 +391,8 @@ class Solver : public SolverBase {
     kp_.plane_big = (long long)d_.ld_big * d_.ny2;
     kp_.dx = d_.dx; kp_.dy = d_.dy; kp_.dz = d_.dz;
     kp_.L_x = d_.p.L_x; kp_.L_y = d_.p.L_y; kp_.L_z = d_.p.L_z;
-    kp_.dt = d_.p.dt; kp_.tadv1 = d_.tadv1; kp_.tadv2 = d_.tadv2;
     kp_.vonk = d_.p.vonk; kp_.zo = d_.p.zo; kp_.nu = d_.nu; kp_.delta = d_.delta;
-    kp_.lagran_dt = d_.lagran_dt; kp_.mpfx = d_.mpfx; kp_.mpfy = d_.mpfy;
+    kp_.mpfx = d_.mpfx; kp_.mpfy = d_.mpfy;
     kp_.nu_nd = d_.p.nu_molec / (d_.p.z_i * d_.p.u_star);
     kp_.ubot = d_.p.ubot; kp_.utop = d_.p.utop;
     kp_.lbc = d_.p.lbc_mom; kp_.ubc = d_.p.ubc_mom; kp_.use_mpf = d_.p.use_mean_p_force;
@@ -417,6 +420,10 @@ class Solver : public SolverBase {
     flags_d_ = alloc<int>(cap_);
     kp_.zo_i = zo_d_;
     kp_.iflags = flags_d_;
+    sc_d_ = alloc<double>((long long)SC_N * cap_);
+    cflmax_d_ = alloc<unsigned long long>(3LL * cap_);
+    tact_d_ = alloc<int>(cap_);
+    kp_.sc = sc_d_;
     // LESGO_GRAPHS=0 replays nothing: every step launches eagerly
     if (const char* g = std::getenv("LESGO_GRAPHS")) graphs_allowed_ = std::strcmp(g, "0") != 0;
     use_graphs_ = graphs_allowed_;
@@ -451,6 +458,7 @@ class Solver : public SolverBase {
     // fresh state: zero every field of the slot, then the seeded IC
     for (int f = 0; f < LESGO_NFIELDS; ++f)
       CK(cudaMemsetAsync(F_[f] + slot * kp_.istride, 0, kp_.istride * sizeof(R), st_));
+    init_step_constants(slot);
     ic_slot(slot, spec.seed);
     CK(cudaStreamSynchronize(st_));
     return sl.id;
@@ -464,6 +472,8 @@ class Solver : public SolverBase {
       for (int f = 0; f < LESGO_NFIELDS; ++f)
         CK(cudaMemcpyAsync(F_[f] + slot * kp_.istride, F_[f] + last * kp_.istride, kp_.istride * sizeof(R),
                            cudaMemcpyDeviceToDevice, st_));
+      CK(cudaMemcpyAsync(sc_d_ + (long long)slot * SC_N, sc_d_ + (long long)last * SC_N, SC_N * sizeof(double),
+                         cudaMemcpyDeviceToDevice, st_));
       if (tacc_)
         for (int f = 0; f < TA_N; ++f)
           CK(cudaMemcpyAsync(tacc_ + f * tacc_stride_ + slot * kp_.istride, tacc_ + f * tacc_stride_ + last * kp_.istride,
@@ -574,7 +584,7 @@ class Solver : public SolverBase {
   void sgs_stag() override {
     need_active();
     bool lag_any = false;
-    upload_flags(false, &lag_any);
+    for (const auto& sl : slots_) lag_any = lag_any || (sl.flags & IF_LAG);
     if (!lag_any) {
       column<COL_STORE_S | COL_TAU>();
     } else {
@@ -625,7 +635,10 @@ class Solver : public SolverBase {
   }
   void begin_step() override {
     need_active();
-    for (auto& sl : slots_) { ++sl.jt; ++sl.jt_total; sl.time += d_.p.dt; }
+    advance_counters();
+    bool lag_any = false;
+    upload_flags(&lag_any);
+    step_begin_kernels();
     for (int c = 0; c < 3; ++c)
       CK(cudaMemcpyAsync(F_[LESGO_RHSX_F + c], F_[LESGO_RHSX + c], kp_.istride * kp_.ninst * sizeof(R),
                          cudaMemcpyDeviceToDevice, st_));
@@ -672,9 +685,9 @@ class Solver : public SolverBase {
   void step(int nsteps) override {
     need_active();
     for (int s = 0; s < nsteps; ++s) {
-      for (auto& sl : slots_) { ++sl.jt; ++sl.jt_total; sl.time += d_.p.dt; }
+      advance_counters();
       bool lag_any = false;
-      const bool special = upload_flags(true, &lag_any);
+      const bool special = upload_flags(&lag_any);
       const int code = (lag_any ? 1 : 0) | (kp_.ninst << 1);
       if (!special && use_graphs_) {
         auto it = graphs_.find(code);
@@ -718,7 +731,11 @@ class Solver : public SolverBase {
     CK(cudaMemsetAsync(tacc_, 0, TA_N * tacc_stride_ * sizeof(double), st_));
     ta_nstart_ = nstart; ta_nend_ = nend; ta_nskip_ = nskip;
     tavg_on_ = true;
-    for (auto& sl : slots_) { sl.ta_init = false; sl.ta_dt = 0.0; sl.ta_total = 0.0; }
+    for (size_t s = 0; s < slots_.size(); ++s) {
+      slots_[s].ta_init = false;
+      write_sc((int)s, SC_TAW, 0.0);
+      write_sc((int)s, SC_TAT, 0.0);
+    }
     CK(cudaStreamSynchronize(st_));
   }
   // output_loop's schedule for each instance after a step: every step of
@@ -727,32 +744,35 @@ class Solver : public SolverBase {
   void tavg_sample() override {
     if (!tavg_on_) throw Error(LESGO_ERR_ARG, "tavg: not configured");
     need_active();
-    std::vector<double> w(slots_.size(), 0.0);
-    bool any = false;
+    // act: 0 nothing, 1 tavg%init, 2 tavg%init from tavg.out, 3 tavg%compute;
+    // the pending weight (dt summed over the window's steps) lives on the device
+    std::vector<int> act(slots_.size(), 0);
+    bool any = false, sample = false;
     for (size_t s = 0; s < slots_.size(); ++s) {
       Slot& sl = slots_[s];
       if (sl.jt_total < ta_nstart_ || sl.jt_total > ta_nend_) continue;
-      sl.ta_dt += d_.p.dt;
       if ((sl.jt_total - ta_nstart_) % ta_nskip_ != 0) continue;
+      any = true;
       if (!sl.ta_init) {
-        // tavg%init: zero sums, or take up the sums read from tavg.out
-        // (which carries no pressure sum: time_average.f90:114-150)
+        // zero the sums, or keep those read from tavg.out (which carries no
+        // pressure sum: time_average.f90:114-150)
         for (int f = 0; f < TA_N; ++f)
           if (!sl.ta_loaded || f == TA_P)
             CK(cudaMemsetAsync(tacc_ + f * tacc_stride_ + s * kp_.istride, 0, kp_.istride * sizeof(double), st_));
+        act[s] = sl.ta_loaded ? 2 : 1;
         sl.ta_init = true;
-        sl.ta_total = sl.ta_loaded ? sl.ta_total_loaded : 0.0;
         sl.ta_loaded = false;
-        sl.ta_dt = 0.0;
       } else {
-        w[s] = sl.ta_dt;
-        sl.ta_total += sl.ta_dt;
-        sl.ta_dt = 0.0;
-        any = true;
+        act[s] = 3;
+        sample = true;
       }
     }
     if (!any) return;
-    CK(cudaMemcpyAsync(tw_d_, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, st_));
+    CK(cudaMemcpyAsync(tact_d_, act.data(), act.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
+    pre();
+    k_tavg_prep<<<(kp_.ninst + 63) / 64, 64, 0, st_>>>(sc_d_, tact_d_, tw_d_, kp_.ninst);
+    post("tavg.prep", 0.0);
+    if (!sample) return;
     TavgArgs<R> a;
     a.u = F_[LESGO_U]; a.v = F_[LESGO_V]; a.w = F_[LESGO_W]; a.p = F_[LESGO_P];
     a.txx = F_[LESGO_TXX]; a.tyy = F_[LESGO_TYY]; a.tzz = F_[LESGO_TZZ];
@@ -771,11 +791,11 @@ class Solver : public SolverBase {
     if (which < 0 || which >= TA_N + 6) throw Error(LESGO_ERR_ARG, "tavg: bad quantity");
     if (lbz < 0 || nzhi > d_.nz || nzhi < lbz) throw Error(LESGO_ERR_ARG, "levels outside 0..nz");
     const int slot = slot_of(id);
-    const Slot& sl = slots_[slot];
-    if (!(sl.ta_total > 0)) throw Error(LESGO_ERR_ARG, "tavg: no sample yet");
+    const double tot = read_sc(slot, SC_TAT);
+    if (!(tot > 0)) throw Error(LESGO_ERR_ARG, "tavg: no sample yet");
     double* stg = staging(kp_.istride);
     const long long n = kp_.istride;
-    k_tavg_get<<<grid1(n), 256, 0, st_>>>(tacc_, tacc_stride_, slot * kp_.istride, which, 1.0 / sl.ta_total, stg, n);
+    k_tavg_get<<<grid1(n), 256, 0, st_>>>(tacc_, tacc_stride_, slot * kp_.istride, which, 1.0 / tot, stg, n);
     post();
     const long long off = (long long)lbz * kp_.plane, cnt = (long long)(nzhi - lbz + 1) * kp_.plane;
     CK(cudaMemcpyAsync(host, stg + off, cnt * sizeof(double), cudaMemcpyDeviceToHost, st_));
@@ -786,11 +806,11 @@ class Solver : public SolverBase {
     if (!tacc_) throw Error(LESGO_ERR_ARG, "tavg: not configured");
     if (which < 0 || which >= TA_N + 6) throw Error(LESGO_ERR_ARG, "tavg: bad quantity");
     const int slot = slot_of(id);
-    const Slot& sl = slots_[slot];
-    if (!(sl.ta_total > 0)) throw Error(LESGO_ERR_ARG, "tavg: no sample yet");
+    const double tot = read_sc(slot, SC_TAT);
+    if (!(tot > 0)) throw Error(LESGO_ERR_ARG, "tavg: no sample yet");
     double* stg = staging(kp_.istride);
     if (!prof_d_) prof_d_ = alloc<double>(d_.nz + 1);
-    k_tavg_get<<<grid1(kp_.istride), 256, 0, st_>>>(tacc_, tacc_stride_, slot * kp_.istride, which, 1.0 / sl.ta_total,
+    k_tavg_get<<<grid1(kp_.istride), 256, 0, st_>>>(tacc_, tacc_stride_, slot * kp_.istride, which, 1.0 / tot,
                                                     stg, kp_.istride);
     post();
     k_plane_mean<<<d_.nz + 1, 256, 0, st_>>>(stg, d_.nx, d_.ny, d_.ld, prof_d_);
@@ -798,8 +818,9 @@ class Solver : public SolverBase {
     CK(cudaMemcpyAsync(prof, prof_d_, (d_.nz + 1) * sizeof(double), cudaMemcpyDeviceToHost, st_));
     CK(cudaStreamSynchronize(st_));
   }
-  double tavg_total_time(int id) const override { return slots_[slot_of(id)].ta_total; }
-  double sim_time(int id) const override { return slots_[slot_of(id)].time; }
+  double tavg_total_time(int id) override { return read_sc(slot_of(id), SC_TAT); }
+  double sim_time(int id) override { return read_sc(slot_of(id), SC_TIME); }
+  double time_step(int id) override { return read_sc(slot_of(id), SC_DT); }
 
   // ---------------- checkpoint / restart (io.f90:1173-1267, initial.f90:20-380) ----
   // The 11 fields of vel.out in record order.
@@ -831,7 +852,8 @@ class Solver : public SolverBase {
         // sums of x < nx at levels 1..nz, (nx, ny, nz) like the reference
         fio::File fl(pre + "tavg.out" + sfx, "wb");
         if (!fl.f) throw fio::IoError{"cannot open " + pre + "tavg.out" + sfx};
-        fio::write_record(fl.f, {{&sl.ta_total, 8}});
+        const double tat = read_sc(slot, SC_TAT);
+        fio::write_record(fl.f, {{&tat, 8}});
         std::vector<double> lev(pl), pk((size_t)d_.nx * d_.ny * d_.nz);
         for (int q : kTavgFile) {
           CK(cudaMemcpyAsync(lev.data(), tacc_ + q * tacc_stride_ + slot * kp_.istride + kp_.plane, pl * sizeof(double),
@@ -844,15 +866,16 @@ class Solver : public SolverBase {
           fio::write_record(fl.f, {{pk.data(), (int64_t)pk.size() * 8}});
         }
       }
-      // cfl written: the current maximum CFL (fixed time step)
+      // cfl written: the CFL number of a varying step, else the current maximum
       double dg[4];
       diag(id, dg);
       fio::TimeDat td;
+      const double t = read_sc(slot, SC_TIME);
       td.jt_total = sl.jt_total;
-      td.total_time = sl.time;
-      td.total_time_dim = sl.time * d_.p.z_i / d_.p.u_star;
-      td.dt = d_.p.dt;
-      td.cfl = dg[2];
+      td.total_time = t;
+      td.total_time_dim = t * d_.p.z_i / d_.p.u_star;
+      td.dt = read_sc(slot, SC_DT);
+      td.cfl = d_.p.use_cfl_dt ? d_.p.cfl : dg[2];
       fio::write_time(pre + "total_time.dat", td);
     } catch (const fio::IoError& e) {
       throw Error(LESGO_ERR_ARG, "checkpoint: " + e.msg);
@@ -919,13 +942,16 @@ class Solver : public SolverBase {
       sl.initu = exact != 0;
       sl.jt = 0;
       sl.flm_init = sl.fqn_init = false;
+      sl.lag_prev = false;
+      init_step_constants(slot);
       if (fio::exists(pre + "total_time.dat")) {
+        // io.f90:73-96: counters and time; with use_cfl_dt also the last dt
         const fio::TimeDat t = fio::read_time(pre + "total_time.dat");
         sl.jt_total = (int)t.jt_total;
-        sl.time = t.total_time;
+        write_sc(slot, SC_TIME, t.total_time);
+        if (d_.p.use_cfl_dt && t.dt > 0) write_sc(slot, SC_DT, t.dt);
       } else {
         sl.jt_total = 0;
-        sl.time = 0.0;
       }
       // time-averaging restart (time_average.f90:114-150)
       std::string tname = pre + "tavg.out";
@@ -934,7 +960,10 @@ class Solver : public SolverBase {
         fio::File fl(tname, "rb");
         std::vector<char> r;
         if (!fio::read_record(fl.f, r) || r.size() != 8) throw fio::IoError{tname + ": no total_time record"};
-        std::memcpy(&sl.ta_total_loaded, r.data(), 8);
+        double tat = 0.0;
+        std::memcpy(&tat, r.data(), 8);
+        write_sc(slot, SC_TAT, tat);
+        write_sc(slot, SC_TAW, 0.0);
         const size_t n3 = (size_t)d_.nx * d_.ny * d_.nz;
         std::vector<double> lev((size_t)pl, 0.0);
         for (int q : kTavgFile) {
@@ -950,8 +979,6 @@ class Solver : public SolverBase {
         }
         sl.ta_loaded = true;
         sl.ta_init = false;
-        sl.ta_dt = 0.0;
-        sl.ta_total = 0.0;
       }
     } catch (const fio::IoError& e) {
       throw Error(LESGO_ERR_ARG, "restart: " + e.msg);
@@ -985,7 +1012,7 @@ class Solver : public SolverBase {
     const double npts = (double)d_.nx * d_.ny * (d_.nz - 1);
     out[0] = h[0] / npts;
     out[1] = h[1] * 0.5 / npts;
-    out[2] = d_.p.dt * std::max({h[2] / d_.dx, h[3] / d_.dy, h[4] / d_.dz});
+    out[2] = read_sc(slot, SC_DT) * std::max({h[2] / d_.dx, h[3] / d_.dy, h[4] / d_.dz});
     const double nxy = (double)d_.nx * d_.ny;
     out[3] = std::sqrt((h[5] / nxy) * (h[5] / nxy) + (h[6] / nxy) * (h[6] / nxy));
   }
@@ -1084,11 +1111,10 @@ class Solver : public SolverBase {
     bool flm_init = false, fqn_init = false;
     int pending = 0;   // IF_INITLM / IF_INITQN set this step (committed after it)
     bool ta_init = false;          // time averaging started (tavg%init done)
-    double ta_dt = 0.0, ta_total = 0.0;
     bool ta_loaded = false;        // sums read from tavg.out, taken up at the first sample
-    double ta_total_loaded = 0.0;
     bool initu = false;            // state read from a checkpoint of this grid (initial.f90:77-84)
-    double time = 0.0;             // total_time
+    bool lag_prev = false;         // the previous step ran the dynamic update
+    int flags = 0;                 // IF_* of the current step
   };
 
   int slot_of(int id) const {
@@ -1109,16 +1135,15 @@ class Solver : public SolverBase {
     CK(cudaStreamSynchronize(st_));
   }
 
-  // Per-instance flags of this step (counters already advanced).  Returns
-  // true when some flag other than IF_LAG is set (a step that is not replayed).
-  bool upload_flags(bool count_euler, bool* lag_any) {
-    std::vector<int> fl(slots_.size(), 0);
-    bool special = false, lag = false;
-    for (size_t s = 0; s < slots_.size(); ++s) {
-      Slot& sl = slots_[s];
+  // Advance every instance's counters by one step and set its flags for the
+  // step (main.f90:146-147, sgs_stag_util.f90:72-217, io.f90:557-562).
+  void advance_counters() {
+    for (auto& sl : slots_) {
+      ++sl.jt;
+      ++sl.jt_total;
       const bool inilag = !sl.initu;
       int f = 0;
-      if (count_euler && sl.jt_total == 1 && !sl.initu) f |= IF_EULER;
+      if (sl.jt_total == 1 && !sl.initu) f |= IF_EULER;
       const bool cs_fill = (sl.jt == 1 && inilag);
       if (cs_fill) f |= IF_CSFILL;
       if (!cs_fill && (sl.jt >= d_.p.dyn_init || sl.initu) && (sl.jt_total % d_.p.cs_count == 0)) {
@@ -1126,14 +1151,72 @@ class Solver : public SolverBase {
         if (inilag && !sl.flm_init && (sl.jt == d_.p.cs_count || sl.jt == d_.p.dyn_init)) f |= IF_INITLM;
         if (inilag && !sl.fqn_init && (sl.jt == d_.p.cs_count || sl.jt == d_.p.dyn_init)) f |= IF_INITQN;
       }
+      if (d_.p.use_cfl_dt) {
+        if (sl.lag_prev) f |= IF_LAGRESET;
+        if (sl.jt >= d_.p.dyn_init - d_.p.cs_count + 1 || sl.initu) f |= IF_LAGACC;
+      }
+      if (tavg_on_ && sl.jt_total >= ta_nstart_ && sl.jt_total <= ta_nend_) f |= IF_TAACC;
+      sl.lag_prev = (f & IF_LAG) != 0;
       sl.pending = f & (IF_INITLM | IF_INITQN);
-      if (f & ~IF_LAG) special = true;
+      sl.flags = f;
+    }
+  }
+  // Upload this step's flags.  Returns true when a flag changes the kernels
+  // the step launches (a step that is not replayed).
+  bool upload_flags(bool* lag_any) {
+    std::vector<int> fl(slots_.size(), 0);
+    bool special = false, lag = false;
+    for (size_t s = 0; s < slots_.size(); ++s) {
+      const int f = slots_[s].flags;
+      if (f & IF_SPECIAL) special = true;
       if (f & IF_LAG) lag = true;
       fl[s] = f;
     }
     CK(cudaMemcpyAsync(flags_d_, fl.data(), fl.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
     *lag_any = lag;
     return special;
+  }
+  // cfl_util.f90:70-111 and main.f90:135-150 on the device: the new dt (with
+  // use_cfl_dt), total_time and the pending time-average weight.
+  void step_begin_kernels() {
+    if (d_.p.use_cfl_dt) {
+      const long long m = (long long)d_.nx * d_.ny * (d_.nz - 1);
+      const int nb = (int)std::max<long long>(1, std::min<long long>((m + 2047) / 2048, 1024));
+      pre();
+      k_cfl_max<R><<<dim3(nb, kp_.ninst), 256, 0, st_>>>(F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_, cflmax_d_);
+      post("step.cfl_max", 3.0 * m * kp_.ninst * sizeof(R));
+    }
+    StepBeginArgs a;
+    a.sc = sc_d_; a.iflags = flags_d_; a.mx = cflmax_d_; a.ninst = kp_.ninst; a.cfl_mode = d_.p.use_cfl_dt ? 1 : 0;
+    a.cfl = d_.p.cfl; a.dx = d_.dx; a.dy = d_.dy; a.dz = d_.dz; a.c1 = 1.0 / ((double)d_.nx * d_.ny);
+    a.z_i = d_.p.z_i; a.u_star = d_.p.u_star; a.T_avg_dim = d_.p.T_avg_dim;
+    pre();
+    k_step_begin<<<(kp_.ninst + 63) / 64, 64, 0, st_>>>(a);
+    post("step.begin", 0.0);
+  }
+  // Step constants of a fresh instance (fixed time step values; with
+  // use_cfl_dt the first step replaces them).
+  void init_step_constants(int slot) {
+    std::vector<double> c(SC_N, 0.0);
+    const double dt = d_.p.dt;
+    c[SC_DT] = dt; c[SC_DTF] = dt;
+    c[SC_T1] = d_.tadv1; c[SC_T2] = d_.tadv2;
+    c[SC_LDT] = d_.p.use_cfl_dt ? 0.0 : d_.lagran_dt;
+    c[SC_PS] = 1.0 / ((double)d_.nx * d_.ny) / d_.tadv1 / dt;
+    const double dt_dim = dt * d_.p.z_i / d_.p.u_star;
+    c[SC_EPS] = d_.p.T_avg_dim > 0 ? (dt_dim / d_.p.T_avg_dim) / (1. + dt_dim / d_.p.T_avg_dim) : 1.0;
+    CK(cudaMemcpyAsync(sc_d_ + (long long)slot * SC_N, c.data(), SC_N * sizeof(double), cudaMemcpyHostToDevice, st_));
+    CK(cudaStreamSynchronize(st_));
+  }
+  double read_sc(int slot, int which) {
+    double v = 0.0;
+    CK(cudaMemcpyAsync(&v, sc_d_ + (long long)slot * SC_N + which, sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    return v;
+  }
+  void write_sc(int slot, int which, double v) {
+    CK(cudaMemcpyAsync(sc_d_ + (long long)slot * SC_N + which, &v, sizeof(double), cudaMemcpyHostToDevice, st_));
+    CK(cudaStreamSynchronize(st_));
   }
   void commit_lagrange_init() {
     for (auto& sl : slots_) {
@@ -1185,8 +1268,8 @@ class Solver : public SolverBase {
     td_.u_d_T = upload_vec(state);
     td_.f_n = alloc<double>(th_.n);
     td_.disk = alloc<double>(th_.n);
-    const double dt_dim = d_.p.dt * d_.p.z_i / d_.p.u_star;
-    td_.eps = d_.p.T_avg_dim > 0 ? (dt_dim / d_.p.T_avg_dim) / (1. + dt_dim / d_.p.T_avg_dim) : 1.0;
+    td_.tinst = upload_vec(th_.tinst);
+    td_.sc = sc_d_;
     td_.dvol = d_.dx * d_.dy * d_.dz;
     cols_ = upload_vec(th_.cols);
     // the applied-force fields are rewritten only on disk nodes: clear them
@@ -1202,6 +1285,7 @@ class Solver : public SolverBase {
   }
 
   void step_body(bool lag_any) {
+    step_begin_kernels();
     // main.f90:155-172: derivatives (RHS_f is saved inside the fused convec epilogue)
     const InstMap im = imf(d_.nz);
     SrcFields<R, 3> src{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, (R)(1.0 / ((double)d_.nx * d_.ny)), 1, 1, d_.ld,
@@ -1561,7 +1645,7 @@ class Solver : public SolverBase {
     dst.Cs = F_[LESGO_CS_OPT2]; dst.Beta = F_[LESGO_BETA]; dst.Tn_all = F_[LESGO_TN_ALL]; dst.ee_now = F_[LESGO_EE_NOW];
     dst.cst = 2.0 * (d_.delta * d_.delta);
     dst.opftdelta = 1.5 * d_.delta;
-    dst.lagran_dt = d_.lagran_dt;
+    dst.sc = sc_d_;
     dst.beta_exp = std::log(2.0) / (std::log(4.0) - std::log(2.0));
     dst.ld = d_.ld; dst.nz = d_.nz; dst.lbc = kp_.lbc; dst.ubc = kp_.ubc;
     dst.iflags = flags_d_;
@@ -1598,7 +1682,7 @@ class Solver : public SolverBase {
       dc.u = F_[LESGO_U]; dc.v = F_[LESGO_V]; dc.w = F_[LESGO_W];
       dc.divtx = F_[LESGO_DIVTX]; dc.divty = F_[LESGO_DIVTY]; dc.divtz = F_[LESGO_DIVTZ];
       dc.fxa = F_[LESGO_FXA]; dc.fya = F_[LESGO_FYA]; dc.fza = F_[LESGO_FZA];
-      dc.dt = d_.p.dt; dc.t1 = d_.tadv1; dc.t2 = d_.tadv2; dc.mpfx = d_.mpfx; dc.mpfy = d_.mpfy;
+      dc.sc = sc_d_; dc.mpfx = d_.mpfx; dc.mpfy = d_.mpfy;
       dc.ld = d_.ld; dc.nz = d_.nz; dc.use_mpf = d_.p.use_mean_p_force; dc.turbines = kp_.turbines;
       dc.iflags = flags_d_; dc.plane = kp_.plane; dc.im = im;
       xinv<3>(dc, specB_, d_.nx, d_.ny, d_.nz, px_, "convec.xinv_ab2", 18 + 3 * kp_.turbines);
@@ -1609,8 +1693,8 @@ class Solver : public SolverBase {
     const int nz = d_.nz, ny = d_.ny;
     const long long pl_s = (long long)ny * d_.K;
     const double c1 = 1.0 / ((double)d_.nx * d_.ny);
-    const R c2 = (R)(c1 / d_.tadv1 / d_.p.dt);
-    SrcFields<R, 3> su{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, c2, 1, 1, d_.ld, kp_.plane, imf(nz)};
+    // scale 1/(nx ny tadv1 dt), the instance's step constant SC_PS
+    SrcFields<R, 3> su{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, (R)0, 1, 1, d_.ld, kp_.plane, imf(nz), sc_d_, SC_PS};
     xfwd<3>(su, d_.nx, ny, nz, specA_, px_, "press.xfwd");
     SrcFields<R, 1> sd{{F_[LESGO_DIVTZ]}, (R)c1, 1, nz - 1, d_.ld, kp_.plane, imf(2)};
     xfwd<1>(sd, d_.nx, ny, 2, specC_, px_, "press.xfwd_bc");
@@ -1635,11 +1719,11 @@ class Solver : public SolverBase {
                                               "press.ypass_inv_bc");
     if (fused) {
       DstPress<R, true> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U],
-                           F_[LESGO_V], d_.p.dt, d_.tadv1, d_.ld, kp_.plane, imf(nz - 1)};
+                           F_[LESGO_V], sc_d_, d_.ld, kp_.plane, imf(nz - 1)};
       xinv<3>(dp, specB_, d_.nx, ny, nz - 1, px_, "press.xinv_project", 9);
     } else {
       DstPress<R, false> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U],
-                            F_[LESGO_V], d_.p.dt, d_.tadv1, d_.ld, kp_.plane, imf(nz - 1)};
+                            F_[LESGO_V], sc_d_, d_.ld, kp_.plane, imf(nz - 1)};
       xinv<3>(dp, specB_, d_.nx, ny, nz - 1, px_);
     }
     DstFields<R, 1> d0{{F_[LESGO_P]}, 0, nz, d_.ld, kp_.plane, imf(2)};
@@ -1687,6 +1771,9 @@ class Solver : public SolverBase {
   double2 *hspec_ = nullptr, *hplane_ = nullptr, *phat_ = nullptr;
   double *ibet_ = nullptr, *tgam_ = nullptr;
   double *tacc_ = nullptr, *tw_d_ = nullptr, *prof_d_ = nullptr;
+  double* sc_d_ = nullptr;                   // step constants [cap][SC_N]
+  unsigned long long* cflmax_d_ = nullptr;   // per-instance |u|, |v|, |w| maxima
+  int* tact_d_ = nullptr;                    // time-averaging action per instance
   long long tacc_stride_ = 0;
   bool tavg_on_ = false;
   int ta_nstart_ = 1, ta_nend_ = 50000, ta_nskip_ = 100;
@@ -1760,6 +1847,7 @@ int lesgo_gpu_params_default(lesgo_params_t* p) {
   p->mean_p_force_x = 1.0; p->mean_p_force_y = 0.0;
   p->precision = LESGO_FP64;
   p->alpha1 = 1.5; p->alpha2 = 1.5; p->filter_cutoff = 1e-2; p->T_avg_dim = -1.0; p->adm_correction = 1;
+  p->use_cfl_dt = 0; p->cfl = (double)0.05f;
   return LESGO_OK;
 }
 
@@ -2174,6 +2262,10 @@ int lesgo_gpu_checkpoint_read_inst(lesgo_handle_t* h, int id, const char* path, 
 int lesgo_gpu_sim_time(lesgo_handle_t* h, int id, double* total_time) {
   if (!total_time) return LESGO_ERR_ARG;
   return guarded(h, [&] { *total_time = h->s->sim_time(id < 0 ? h->inst0 : id); });
+}
+int lesgo_gpu_time_step(lesgo_handle_t* h, int id, double* dt) {
+  if (!dt) return LESGO_ERR_ARG;
+  return guarded(h, [&] { *dt = h->s->time_step(id < 0 ? h->inst0 : id); });
 }
 }  // extern "C"
 

@@ -11,7 +11,7 @@ struct KP {
   int nx, ny, nz, ld, lh, nx2, ny2, ld_big, K;  // K = nx/2 kept x modes
   long long plane, plane_big;                   // elements per (ld,ny) / (ld_big,ny2) plane
   double dx, dy, dz, L_x, L_y, L_z;
-  double dt, tadv1, tadv2, vonk, zo, nu, delta, lagran_dt;
+  double vonk, zo, nu, delta;
   double mpfx, mpfy, nu_nd, ubot, utop;
   int lbc, ubc, use_mpf, turbines;
   int ninst;                 // instances (slots) stacked in every field
@@ -19,12 +19,31 @@ struct KP {
   long long istride_big;     // same on the 3/2 grid
   const double* zo_i;        // per-instance roughness length
   const int* iflags;         // per-instance step flags (IF_*)
+  const double* sc;          // per-instance step constants [inst][SC_N] (SC_*)
+};
+
+// Per-instance step constants, resident on the device so that a time step
+// chosen on the device (cfl_util.f90:70-111) reaches every kernel of a
+// replayed step: dt, the AB2 weights tadv1/tadv2 (main.f90:135-144),
+// lagran_dt (sgs_stag_util.f90:72-83), the pressure-RHS scale
+// 1/(nx ny tadv1 dt) (press_stag_array.f90:52), the disk-velocity filter
+// weight of the turbines (turbines.f90:520-530), total_time, and the
+// time-averaging weight pending and its sum (time_average.f90).
+enum : int {
+  SC_DT = 0, SC_T1, SC_T2, SC_LDT, SC_PS, SC_EPS, SC_TIME, SC_TAW, SC_TAT, SC_DTF, SC_N = 16
 };
 
 // Per-instance step flags: Euler first step (main.f90:273-280), Cs_opt2 =
 // 0.03 (sgs_stag_util.f90:187-189), dynamic update due this step
 // (:192-217), F_LM/F_MM and F_QN/F_NN initialisation (lagrange_Sdep.f90:266-276, 326-336).
 enum : int { IF_EULER = 1, IF_CSFILL = 2, IF_LAG = 4, IF_INITLM = 8, IF_INITQN = 16 };
+// Flags read only by the step-begin kernel: the step counts toward the
+// pending time-average weight (io.f90:559-562); lagran_dt accumulates dt
+// (sgs_stag_util.f90:74-79); lagran_dt restarts from zero after the previous
+// step's dynamic update (lagrange_Sdep.f90:430).
+enum : int { IF_TAACC = 32, IF_LAGACC = 64, IF_LAGRESET = 128 };
+// Flags that change which kernels a step launches (such steps are not replayed).
+constexpr int IF_SPECIAL = IF_EULER | IF_CSFILL | IF_INITLM | IF_INITQN;
 
 // Launch level index li -> (instance, level within the instance).
 struct InstMap {
@@ -40,6 +59,7 @@ struct InstMap {
 // Xf row loaders
 // ---------------------------------------------------------------------------
 // NF fields scaled by one constant, at levels lev0 + li*levstride.
+// With `isc` set, the scale is the instance's step constant isc[inst][isc_idx].
 template <typename R, int NF>
 struct SrcFields {
   const R* p[NF];
@@ -47,9 +67,12 @@ struct SrcFields {
   int lev0, levstride, ld;
   long long plane;
   InstMap im;
+  const double* isc = nullptr;
+  int isc_idx = 0;
   __device__ __forceinline__ void load2(int n, int jy, int li, cplx<R>* v) const {
     const int inst = im.inst(li), lv = li - inst * im.nli;
     const long long off = inst * im.istr + (long long)(lev0 + lv * levstride) * plane + (long long)jy * ld + 2 * n;
+    const R scale = isc ? (R)isc[inst * SC_N + isc_idx] : this->scale;
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       cplx<R> a = *reinterpret_cast<const cplx<R>*>(p[f] + off);
@@ -296,7 +319,8 @@ template <typename R, bool FUSED>
 struct DstConvec {
   R *RHSx, *RHSy, *RHSz, *RHSxf, *RHSyf, *RHSzf, *u, *v, *w;
   const R *divtx, *divty, *divtz, *fxa, *fya, *fza;
-  double dt, t1, t2, mpfx, mpfy;
+  const double* sc;   // step constants
+  double mpfx, mpfy;
   int ld, nz, use_mpf, turbines;
   const int* iflags;
   long long plane;
@@ -310,7 +334,8 @@ struct DstConvec {
       RHSz[q] = vals[2];
       return;
     }
-    const R dtr = (R)dt, t1r = (R)t1, t2r = (R)t2;
+    const double* c = sc + inst * SC_N;
+    const R dtr = (R)c[SC_DT], t1r = (R)c[SC_T1], t2r = (R)c[SC_T2];
     const bool euler = (iflags[inst] & IF_EULER) != 0;
     if (k <= nz - 1) {
       R nxr = -vals[0] - divtx[q];
@@ -339,7 +364,7 @@ struct DstConvec {
 template <typename R, bool FUSED>
 struct DstPress {
   R *p, *dpdx, *dpdy, *RHSx, *RHSy, *u, *v;
-  double dt, t1;
+  const double* sc;   // step constants
   int ld;
   long long plane;
   InstMap im;
@@ -353,7 +378,8 @@ struct DstPress {
       dpdy[q] = vals[2];
       return;
     }
-    const R dtr = (R)dt, t1r = (R)t1;
+    const double* c = sc + inst * SC_N;
+    const R dtr = (R)c[SC_DT], t1r = (R)c[SC_T1];
     RHSx[q] = RHSx[q] - vals[1];
     RHSy[q] = RHSy[q] - vals[2];
     u[q] = u[q] + dtr * (-t1r * vals[1]);
@@ -369,7 +395,8 @@ template <typename R>
 struct DstLagrange {
   const R *FLMi, *FMMi, *FQNi, *FNNi;  // interpolated running averages
   R *FLM, *FMM, *FQN, *FNN, *Cs, *Beta, *Tn_all, *ee_now;
-  double cst, opftdelta, lagran_dt, beta_exp;
+  double cst, opftdelta, beta_exp;
+  const double* sc;   // step constants (lagran_dt)
   int ld, nz, lbc, ubc;
   const int* iflags;
   long long plane;
@@ -413,7 +440,8 @@ struct DstLagrange {
     R Tn = max(fLM * fMM, zero);
     Tn = (R)opftdelta * pow(Tn, (R)(-1.0 / 8.0));
     Tn = max(zero, Tn);
-    R dumfac = (R)lagran_dt / Tn;
+    const R ldt = (R)sc[inst * SC_N + SC_LDT];
+    R dumfac = ldt / Tn;
     R epsi = dumfac / ((R)1 + dumfac);
     fLM = epsi * LM + ((R)1 - epsi) * fLM;
     fMM = epsi * MM + ((R)1 - epsi) * fMM;
@@ -424,7 +452,7 @@ struct DstLagrange {
     Tn = max(fQN * fNN, zero);
     Tn = (R)opftdelta * pow(Tn, (R)(-1.0 / 8.0));
     Tn = max(zero, Tn);
-    dumfac = (R)lagran_dt / Tn;
+    dumfac = ldt / Tn;
     epsi = dumfac / ((R)1 + dumfac);
     fQN = epsi * QN + ((R)1 - epsi) * fQN;
     fNN = epsi * NN + ((R)1 - epsi) * fNN;

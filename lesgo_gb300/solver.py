@@ -41,7 +41,7 @@ PARAM_DEFAULTS = dict(
     ifilter=1, lbc_mom=2, ubc_mom=0, molec=False, nu_molec=1.14e-5, ubot=0.0, utop=0.0,
     use_mean_p_force=True, eval_mean_p_force=True, mean_p_force_x=1.0, mean_p_force_y=0.0,
     initu=False, precision="fp64", alpha1=1.5, alpha2=1.5, filter_cutoff=1e-2, T_avg_dim=-1.0,
-    adm_correction=True,
+    adm_correction=True, use_cfl_dt=False, cfl=0.05,
 )
 
 
@@ -54,11 +54,11 @@ def make_params(**kw) -> L.Params:
     p = L.Params()
     p.nx, p.ny, p.nz_tot = cfg["nx"], cfg["ny"], cfg["Nz"]
     for name in ("L_x", "L_y", "L_z", "z_i", "u_star", "vonk", "zo", "dt", "nu_molec", "ubot", "utop",
-                 "mean_p_force_x", "mean_p_force_y", "alpha1", "alpha2", "filter_cutoff", "T_avg_dim"):
+                 "mean_p_force_x", "mean_p_force_y", "alpha1", "alpha2", "filter_cutoff", "T_avg_dim", "cfl"):
         setattr(p, name, float(cfg[name]))
     for name in ("sgs_model", "cs_count", "dyn_init", "ifilter", "lbc_mom", "ubc_mom"):
         setattr(p, name, int(cfg[name]))
-    for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction"):
+    for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction", "use_cfl_dt"):
         setattr(p, name, 1 if cfg[name] else 0)
     prec = cfg["precision"]
     p.precision = {"fp64": L.LESGO_FP64, "mixed": L.LESGO_MIXED}[prec] if isinstance(prec, str) else int(prec)
@@ -92,8 +92,9 @@ def read_conf(path: str, with_turbines: bool = True, max_turbines: int = 4096):
         kw[name] = getattr(p, name)
     for name in ("sgs_model", "cs_count", "dyn_init", "ifilter", "lbc_mom", "ubc_mom"):
         kw[name] = getattr(p, name)
-    for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction"):
+    for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction", "use_cfl_dt"):
         kw[name] = bool(getattr(p, name))
+    kw["cfl"] = p.cfl
     kw["turbines"] = [{k: getattr(tb[i], k) for k, _ in L.Turbine._fields_} for i in range(p.n_turbines)]
     rd = {k: getattr(run, k) for k, _ in L.Run._fields_}
     return kw, rd, log.value.decode()
@@ -340,6 +341,12 @@ class LesgoGPU:
         self._check(self._lib.lesgo_gpu_checkpoint_read(self._h, os.fsencode(path), C.byref(same)))
         return bool(same.value)
 
+    def time_step(self) -> float:
+        """dt of the last step (chosen on the device with use_cfl_dt)."""
+        t = C.c_double()
+        self._check(self._lib.lesgo_gpu_time_step(self._h, -1, C.byref(t)))
+        return t.value
+
     def sim_time(self) -> float:
         t = C.c_double()
         self._check(self._lib.lesgo_gpu_sim_time(self._h, -1, C.byref(t)))
@@ -486,6 +493,12 @@ class LesgoBatch:
         same = C.c_int()
         self._check(self._lib.lesgo_gpu_checkpoint_read_inst(self._h, iid, os.fsencode(path), C.byref(same)))
         return bool(same.value)
+
+    def time_step(self, iid: int) -> float:
+        """dt of the last step (chosen on the device with use_cfl_dt)."""
+        t = C.c_double()
+        self._check(self._lib.lesgo_gpu_time_step(self._h, iid, C.byref(t)))
+        return t.value
 
     def sim_time(self, iid: int) -> float:
         t = C.c_double()

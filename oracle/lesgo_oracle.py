@@ -72,6 +72,8 @@ class Params:
     mean_p_force_y_in: float = 0.0
     initu: bool = False
     turbines: Optional["TurbineFarm"] = None
+    use_cfl_dt: bool = False
+    cfl: float = float(np.float32(0.05))    # param.f90: a default-real literal
 
     def __post_init__(self):
         nproc = 1
@@ -102,6 +104,8 @@ class Params:
         self.nu = self.nu_molec / (self.u_star * self.z_i) if self.molec else 0.0
         # sgs_stag_util.f90:60-62 (fixed dt)
         self.lagran_dt = float(self.cs_count) * self.dt
+        if self.use_cfl_dt:
+            self.lagran_dt = 0.0                # sgs_param.f90:51, accumulated per step
 
 
 # --------------------------------------------------------------------------
@@ -558,11 +562,15 @@ class Oracle:
         if p.sgs_model != 5:
             raise NotImplementedError("only the Lagrangian scale-dependent model (5)")
         self.calc_Sij()
+        if p.use_cfl_dt and (self.jt >= p.dyn_init - p.cs_count + 1 or p.initu):
+            p.lagran_dt += p.dt                                       # :72-83
         inilag = not p.initu
         if self.jt == 1 and inilag:                                   # :187-189
             self.Cs_opt2[:] = 0.03
         elif (self.jt >= p.dyn_init or p.initu) and (self.jt_total % p.cs_count == 0):
             self.lagrange_Sdep()                                      # :192-217
+            if p.use_cfl_dt:
+                p.lagran_dt = 0.0                                     # lagrange_Sdep.f90:430
         l2 = p.delta ** 2
         X = np.s_[1:nz + 1, :, :nx]
         S = np.sqrt(2.0 * (self.S11[X] ** 2 + self.S22[X] ** 2 + self.S33[X] ** 2
@@ -1151,8 +1159,28 @@ class Oracle:
     def set_ic(self, seed: int):
         self.u, self.v, self.w = initial_condition(self.p, seed)
 
+    def get_cfl_dt(self):
+        """cfl_util.f90:70-111."""
+        p = self.p
+        K = np.s_[1:p.nz, :, :p.nx]
+        iu = np.max(np.abs(self.u[K])) / p.dx
+        iv = np.max(np.abs(self.v[K])) / p.dy
+        iw = np.max(np.abs(self.w[K])) / p.dz
+        m = iu
+        if iv > m:
+            m = iv
+        if iw > m:
+            m = iw
+        return float(p.cfl / m)
+
     def begin_step(self):
-        """main.f90:143-157."""
+        """main.f90:135-157."""
+        p = self.p
+        if p.use_cfl_dt:
+            dt_f = p.dt
+            p.dt = self.get_cfl_dt()
+            p.tadv1 = 1.0 + 0.5 * p.dt / dt_f
+            p.tadv2 = 1.0 - p.tadv1
         self.jt_total += 1
         self.jt += 1
         self.time += self.p.dt
@@ -1411,7 +1439,7 @@ def write_checkpoint(o: "Oracle", prefix: str, ta: Optional["TimeAverage"] = Non
                 f.write(fortran_record_bytes(np.ascontiguousarray(ta.acc[n][1:]).tobytes()))
     with open(prefix + "total_time.dat", "w") as f:
         f.write(" %d %.17E %.17E %.17E %.17E\n" % (o.jt_total, o.time, o.time * p.z_i / p.u_star, p.dt,
-                                                  o.max_cfl()))
+                                                  p.cfl if p.use_cfl_dt else o.max_cfl()))
 
 
 def oracle_state(o: "Oracle", name: str) -> np.ndarray:
@@ -1539,6 +1567,8 @@ def read_checkpoint(o: "Oracle", prefix: str, ta: Optional["TimeAverage"] = None
             oracle_state(o, n)[1:] = 0.0
         o.u[1:], o.v[1:], o.w[1:] = u, v, w
     p.initu = exact
+    if p.use_cfl_dt:
+        p.lagran_dt = 0.0
     o.jt = 0
     o.F_LM_MM_init = o.F_QN_NN_init = False
     o.jt_total, o.time = 0, 0.0
@@ -1546,6 +1576,8 @@ def read_checkpoint(o: "Oracle", prefix: str, ta: Optional["TimeAverage"] = None
         with open(prefix + "total_time.dat") as f:
             vals = f.read().replace(",", " ").replace("D", "E").split()
         o.jt_total, o.time = int(vals[0]), float(vals[1])
+        if p.use_cfl_dt:
+            p.dt = float(vals[3])                     # io.f90:91-94
     tname = prefix + "tavg.out"
     if not os.path.exists(tname):
         tname += ".c0"

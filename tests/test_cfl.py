@@ -1,0 +1,174 @@
+"""Dynamic CFL time step (cfl_util.f90:70-111, main.f90:135-144) with the
+varying-step AB2 weights, lagran_dt accumulated between dynamic updates
+(sgs_stag_util.f90:72-83, lagrange_Sdep.f90:430) and the dt-dependent
+turbine filter weight (turbines.f90:520-530).
+
+The CPU test pins the oracle's schedule of dt and lagran_dt; the GPU tests
+compare the device-chosen time step and the fields with the oracle, the
+drop-in sequence with the fused step, batch instances (each with its own
+dt) with the same instances alone, and a restart from a checkpoint with the
+uninterrupted run.
+"""
+import numpy as np
+import pytest
+
+from oracle.lesgo_oracle import Oracle, Params, TimeAverage
+
+# dyn_init a multiple of cs_count: the Lagrangian averages are initialised at
+# the first dynamic update (lagrange_Sdep.f90:266-276).  Otherwise they start
+# from zero and Cs = F_LM / F_MM amplifies round-off (a 1e-13 change grows to
+# 1e-8 in 12 steps in the oracle alone), which no parity bar survives.
+BASE = dict(nx=32, ny=32, Nz=24, dyn_init=6, cs_count=3, use_cfl_dt=True, cfl=0.05)
+
+
+def test_oracle_cfl_schedule(monkeypatch):
+    """dt = cfl / max(|u|/dx, |v|/dy, |w|/dz) at every step start; tadv1 =
+    1 + dt/(2 dt_prev); lagran_dt sums dt from jt = dyn_init - cs_count + 1
+    and restarts after each dynamic update."""
+    p = Params(nx=16, ny=16, Nz=8, **{k: v for k, v in BASE.items() if k not in ("nx", "ny", "Nz")})
+    o = Oracle(p)
+    o.set_ic(2)
+    seen = []
+    monkeypatch.setattr(o, "lagrange_Sdep", lambda: seen.append((o.jt, p.lagran_dt)))
+    dts = []
+    for _ in range(9):
+        dt_prev = p.dt
+        expect = o.get_cfl_dt()
+        o.step()
+        assert p.dt == expect
+        assert p.tadv1 == 1.0 + 0.5 * p.dt / dt_prev and p.tadv2 == 1.0 - p.tadv1
+        dts.append(p.dt)
+    # dynamic updates at jt = 6 and 9 (jt >= 6, jt_total % 3 == 0)
+    assert [j for j, _ in seen] == [6, 9]
+    assert seen[0][1] == pytest.approx(sum(dts[3:6]), rel=1e-15)    # jt = 4..6
+    assert seen[1][1] == pytest.approx(sum(dts[6:9]), rel=1e-15)    # jt = 7..9
+    assert o.time == pytest.approx(sum(dts), rel=1e-15)
+    assert len(set(dts)) > 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 2e-4)])
+def test_gpu_cfl_matches_oracle(built_lib, precision, tol):
+    from gpu_util import oracle_field, rel_err
+    from lesgo_gb300.solver import LesgoGPU
+    p = Params(**BASE)
+    o = Oracle(p)
+    o.set_ic(1)
+    g = LesgoGPU(precision=precision, **BASE)
+    g.init_ic(1)
+    for _ in range(12):
+        o.step()
+    g.step(12)
+    dtol = 1e-13 if precision == "fp64" else 1e-5
+    assert g.time_step() == pytest.approx(p.dt, rel=dtol)
+    assert g.sim_time() == pytest.approx(o.time, rel=dtol)
+    assert p.dt != 2e-4
+    for f in ("u", "v", "w", "p", "Cs_opt2"):
+        e = rel_err(p, f, g.get(f), oracle_field(o, f))
+        # Cs^2 = <LM>/<MM> is a ratio of FP32 contractions: 5x the field bar
+        assert e < (5 * tol if f == "Cs_opt2" and precision == "mixed" else tol), (f, e)
+    g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_cfl_dropin_equals_fused(built_lib):
+    from lesgo_gb300.solver import LesgoGPU
+    a = LesgoGPU(**BASE)
+    a.init_ic(3)
+    a.step(8)
+    b = LesgoGPU(**BASE)
+    b.init_ic(3)
+    for _ in range(8):
+        b.step_reference_order()
+    assert a.time_step() == b.time_step() and a.sim_time() == b.sim_time()
+    for f in ("u", "v", "w"):
+        x, y = a.get(f)[1:a.nz, :, :a.nx], b.get(f)[1:b.nz, :, :b.nx]
+        assert np.max(np.abs(x - y)) <= 1e-12 * np.max(np.abs(y)), f
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_gpu_cfl_turbines_and_tavg_match_oracle(built_lib):
+    """A time-filtered disk velocity (T_avg_dim > 0: weight from each step's
+    dt) and time averages weighted by the varying dt."""
+    from gpu_util import oracle_field, rel_err
+    from lesgo_gb300.solver import LesgoGPU
+    from test_gpu_parity import _farm
+    ts, farm = _farm(2, 1)
+    farm.T_avg_dim = 50.0
+    kw = dict(BASE, nx=64, ny=32, Nz=24)
+    p = Params(turbines=farm, **kw)
+    o = Oracle(p)
+    o.set_ic(4)
+    ta = TimeAverage(o, 2, 100, 3)
+    g = LesgoGPU(turbines=ts, T_avg_dim=50.0, **kw)
+    g.init_ic(4)
+    g.tavg_config(2, 100, 3)
+    for _ in range(8):
+        o.step()
+        ta.after_step()
+    g.step(8)
+    for f in ("u", "w", "fxa"):
+        e = rel_err(p, f, g.get(f), oracle_field(o, f))
+        assert e < 1e-10, (f, e)
+    po = o.turbine_power()
+    assert np.max(np.abs(g.turbine_state()["power"] - po)) <= 1e-10 * np.max(np.abs(po))
+    assert g.tavg_total_time() == pytest.approx(ta.total_time, rel=1e-13)
+    for name in ("u", "upwp", "fx"):
+        ref = ta.mean(name)[1:p.nz]
+        a = g.tavg_get(name)[:p.nz - 1, :, :p.nx]
+        assert np.max(np.abs(a - ref)) <= 1e-10 * np.max(np.abs(ref)), name
+    g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_cfl_batch_instances_equal_alone(built_lib):
+    """Instances of a batch choose their own dt; each equals its run alone."""
+    from lesgo_gb300.solver import LesgoBatch, LesgoGPU
+    b = LesgoBatch(capacity=3, **BASE)
+    specs = [(1e-4, 31), (5e-4, 32), (2e-5, 33)]
+    ids = [b.add(zo, seed) for zo, seed in specs]
+    b.step(4)
+    b.remove(ids[0])
+    b.step(3)
+    dts = set()
+    for (zo, seed), iid in zip(specs[1:], ids[1:]):
+        g = LesgoGPU(zo=zo, **BASE)
+        g.init_ic(seed)
+        g.step(7)
+        assert b.time_step(iid) == g.time_step()
+        assert b.sim_time(iid) == g.sim_time()
+        dts.add(g.time_step())
+        for f in ("u", "v", "w", "F_LM"):
+            assert np.array_equal(b.get(iid, f)[1:g.nz], g.get(f)[1:g.nz]), (iid, f)
+        g.close()
+    assert len(dts) == 2
+    b.close()
+
+
+@pytest.mark.gpu
+def test_gpu_cfl_restart_is_bitwise(built_lib, tmp_path):
+    """total_time.dat carries the last dt (io.f90:91-94): a restarted run
+    continues with the same AB2 weights and lagran_dt starting from zero, as
+    the reference does."""
+    import os
+    from lesgo_gb300.solver import LesgoGPU
+    pre = str(tmp_path) + os.sep
+    kw = dict(BASE, dyn_init=2, cs_count=1)   # lagran_dt = dt at every update: no state lost at a restart
+    a = LesgoGPU(**kw)
+    a.init_ic(5)
+    a.step(10)
+    b = LesgoGPU(**kw)
+    b.init_ic(5)
+    b.step(5)
+    b.checkpoint_write(pre)
+    c = LesgoGPU(**kw)
+    c.checkpoint_read(pre)
+    assert c.time_step() == b.time_step()
+    c.step(5)
+    assert c.time_step() == a.time_step()
+    for f in ("u", "v", "w", "p"):
+        assert np.array_equal(a.get(f)[1:a.nz], c.get(f)[1:c.nz]), f
+    for h in (a, b, c):
+        h.close()
