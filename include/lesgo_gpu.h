@@ -251,6 +251,17 @@ int lesgo_gpu_turbine_state_inst(lesgo_handle_t* h, int id, double* u_d_T, doubl
 /* Device bytes a handle of this grid and capacity allocates (admission). */
 int lesgo_gpu_footprint(const lesgo_params_t* p, int capacity, long long* bytes);
 
+/* ---- diagnostics log (main.f90:359-436: the wbase / nenergy output) -----
+ * After every step whose jt_total is a multiple of `every`, each instance
+ * appends one row (jt_total, total_time, rmsdiv, ke, cfl, tau_wall_bot)
+ * computed on the device, with no host synchronisation, to a ring of
+ * `capacity` rows.  lesgo_gpu_diag_log_read copies the newest min(rows
+ * written, capacity, maxrows) rows, oldest first, 6 doubles each.
+ * lesgo_gpu_diag_log_sample applies the schedule once now (drop-in callers). */
+int lesgo_gpu_diag_log_config(lesgo_handle_t* h, int every, int capacity);
+int lesgo_gpu_diag_log_sample(lesgo_handle_t* h);
+int lesgo_gpu_diag_log_read(lesgo_handle_t* h, int id, double* rows, int maxrows, int* nrows);
+
 /* ---- time-averaging statistics (time_average.f90; schedule io.f90:557-580)
  * After every step, per instance: steps jt_total in [nstart, nend] add dt to
  * the pending weight; a step with (jt_total - nstart) % nskip == 0 starts the

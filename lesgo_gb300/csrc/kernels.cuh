@@ -742,6 +742,27 @@ __global__ void k_diag_final(const double* partial, int nblocks, double* out) {
   for (int s = 0; s < 7; ++s) out[s] = acc[s];
 }
 
+// The same reduction into one row of an instance's diagnostics log, with the
+// host-side formulas of lesgo_gpu_diag applied on the device (rmsdiv.f90,
+// io.f90:99-141, cfl_util.f90:35-64, functions.f90:882-905): jt_total,
+// total_time, rmsdiv, ke, cfl, tau_wall_bot.
+__global__ void k_diag_log_final(const double* partial, int nblocks, const double* sc_row, double* row,
+                                 double jt_total, double npts, double nxy, double dx, double dy, double dz) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < nblocks; ++b)
+    for (int s = 0; s < 7; ++s) {
+      const double x = partial[b * 7 + s];
+      if (s >= 2 && s <= 4) acc[s] = fmax(acc[s], x); else acc[s] += x;
+    }
+  row[0] = jt_total;
+  row[1] = sc_row[SC_TIME];
+  row[2] = acc[0] / npts;
+  row[3] = acc[1] * 0.5 / npts;
+  row[4] = sc_row[SC_DT] * fmax(fmax(acc[2] / dx, acc[3] / dy), acc[4] / dz);
+  row[5] = sqrt((acc[5] / nxy) * (acc[5] / nxy) + (acc[6] / nxy) * (acc[6] / nxy));
+}
+
 // ---------------------------------------------------------------------------
 // Actuator disks (turbines.f90:465-638).  Node lists are static; the
 // reduction is one block per turbine, the scatter writes each node once with

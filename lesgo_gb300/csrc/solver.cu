@@ -360,6 +360,9 @@ class SolverBase {
   virtual int checkpoint_read(int id, const std::string& path) = 0;
   virtual double sim_time(int id) = 0;
   virtual double time_step(int id) = 0;
+  virtual void diag_log_config(int every, int capacity) = 0;
+  virtual void diag_log_sample() = 0;
+  virtual int diag_log_read(int id, double* out, int maxrows) = 0;
 };
 
 // Device bytes of a handle (the admission footprint of a batch).
@@ -474,6 +477,9 @@ class Solver : public SolverBase {
                            cudaMemcpyDeviceToDevice, st_));
       CK(cudaMemcpyAsync(sc_d_ + (long long)slot * SC_N, sc_d_ + (long long)last * SC_N, SC_N * sizeof(double),
                          cudaMemcpyDeviceToDevice, st_));
+      if (dlog_)
+        CK(cudaMemcpyAsync(dlog_ + (long long)slot * dlog_cap_ * 6, dlog_ + (long long)last * dlog_cap_ * 6,
+                           (size_t)dlog_cap_ * 6 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
       if (tacc_)
         for (int f = 0; f < TA_N; ++f)
           CK(cudaMemcpyAsync(tacc_ + f * tacc_stride_ + slot * kp_.istride, tacc_ + f * tacc_stride_ + last * kp_.istride,
@@ -717,6 +723,7 @@ class Solver : public SolverBase {
       }
       commit_lagrange_init();
       if (tavg_on_) tavg_sample();
+      if (dlog_every_) diag_log_sample();
     }
   }
 
@@ -1017,6 +1024,56 @@ class Solver : public SolverBase {
     out[3] = std::sqrt((h[5] / nxy) * (h[5] / nxy) + (h[6] / nxy) * (h[6] / nxy));
   }
 
+  // ---------------- diagnostics log (main.f90:359-436: wbase / nenergy) -----
+  void diag_log_config(int every, int capacity) override {
+    if (every < 1 || capacity < 1) throw Error(LESGO_ERR_ARG, "diag log: every and capacity must be >= 1");
+    if (!diag_part_) { diag_part_ = alloc<double>(4 * 152 * 7); diag_out_ = alloc<double>(8); }
+    if (capacity != dlog_cap_) {
+      dlog_ = alloc<double>((long long)cap_ * capacity * 6);
+      dlog_cap_ = capacity;
+    }
+    dlog_every_ = every;
+    for (auto& sl : slots_) sl.dlog_count = 0;
+  }
+  // A row for every instance whose jt_total is a multiple of `every`.
+  void diag_log_sample() override {
+    if (!dlog_every_) throw Error(LESGO_ERR_ARG, "diag log: not configured");
+    const int nb = 4 * 152;
+    const double npts = (double)d_.nx * d_.ny * (d_.nz - 1), nxy = (double)d_.nx * d_.ny;
+    for (size_t s = 0; s < slots_.size(); ++s) {
+      Slot& sl = slots_[s];
+      if (sl.jt_total % dlog_every_ != 0) continue;
+      double* row = dlog_ + ((long long)s * dlog_cap_ + sl.dlog_count % dlog_cap_) * 6;
+      pre();
+      k_diag<R><<<nb, 256, 0, st_>>>(F_[LESGO_DUDX], F_[LESGO_DVDY], F_[LESGO_DWDZ], F_[LESGO_U], F_[LESGO_V],
+                                     F_[LESGO_W], F_[LESGO_TXZ], F_[LESGO_TYZ], kp_, diag_part_, (int)s);
+      post("diag.reduce", (double)kp_.plane * d_.nz * 8 * sizeof(R));
+      pre();
+      k_diag_log_final<<<1, 32, 0, st_>>>(diag_part_, nb, sc_d_ + (long long)s * SC_N, row, (double)sl.jt_total, npts,
+                                          nxy, d_.dx, d_.dy, d_.dz);
+      post("diag.log", 0.0);
+      ++sl.dlog_count;
+    }
+  }
+  int diag_log_read(int id, double* out, int maxrows) override {
+    if (!dlog_every_) throw Error(LESGO_ERR_ARG, "diag log: not configured");
+    const int slot = slot_of(id);
+    const Slot& sl = slots_[slot];
+    const int n = (int)std::min<long long>(sl.dlog_count, dlog_cap_);
+    const int m = std::min(n, maxrows);
+    std::vector<double> all((size_t)dlog_cap_ * 6);
+    CK(cudaMemcpyAsync(all.data(), dlog_ + (long long)slot * dlog_cap_ * 6, all.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    // oldest first: the ring's first row is count % cap once it has wrapped
+    const long long first = sl.dlog_count > dlog_cap_ ? sl.dlog_count % dlog_cap_ : 0;
+    for (int r = 0; r < m; ++r) {
+      const long long src = (first + (n - m) + r) % dlog_cap_;
+      std::memcpy(out + 6 * r, all.data() + 6 * src, 6 * sizeof(double));
+    }
+    return m;
+  }
+
   void counters(int id, int* jt, int* jt_total) const override {
     const Slot& sl = slots_[slot_of(id)];
     if (jt) *jt = sl.jt;
@@ -1115,6 +1172,7 @@ class Solver : public SolverBase {
     bool initu = false;            // state read from a checkpoint of this grid (initial.f90:77-84)
     bool lag_prev = false;         // the previous step ran the dynamic update
     int flags = 0;                 // IF_* of the current step
+    long long dlog_count = 0;      // rows written to the diagnostics log
   };
 
   int slot_of(int id) const {
@@ -1774,6 +1832,8 @@ class Solver : public SolverBase {
   double* sc_d_ = nullptr;                   // step constants [cap][SC_N]
   unsigned long long* cflmax_d_ = nullptr;   // per-instance |u|, |v|, |w| maxima
   int* tact_d_ = nullptr;                    // time-averaging action per instance
+  double* dlog_ = nullptr;                   // diagnostics log [cap][dlog_cap_][6]
+  int dlog_cap_ = 0, dlog_every_ = 0;
   long long tacc_stride_ = 0;
   bool tavg_on_ = false;
   int ta_nstart_ = 1, ta_nend_ = 50000, ta_nskip_ = 100;
@@ -2291,3 +2351,17 @@ extern "C" int lesgo_gpu_read_conf(const char* path, int with_turbines, lesgo_pa
     return LESGO_ERR_ARG;
   }
 }
+
+// ---------------------------------------------------------------------------
+// Diagnostics log
+// ---------------------------------------------------------------------------
+extern "C" {
+int lesgo_gpu_diag_log_config(lesgo_handle_t* h, int every, int capacity) {
+  return guarded(h, [&] { h->s->diag_log_config(every, capacity); });
+}
+int lesgo_gpu_diag_log_sample(lesgo_handle_t* h) { return guarded(h, [&] { h->s->diag_log_sample(); }); }
+int lesgo_gpu_diag_log_read(lesgo_handle_t* h, int id, double* rows, int maxrows, int* nrows) {
+  if (!rows || !nrows || maxrows < 0) return LESGO_ERR_ARG;
+  return guarded(h, [&] { *nrows = h->s->diag_log_read(id < 0 ? h->inst0 : id, rows, maxrows); });
+}
+}  // extern "C"

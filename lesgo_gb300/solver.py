@@ -310,6 +310,21 @@ class LesgoGPU:
     def launches_per_step(self, with_sgs_update: bool = False) -> int:
         return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
 
+    # ---------------- diagnostics log ---------------------------------------------------
+    def diag_log_config(self, every: int, capacity: int = 1024):
+        """Rows of (jt_total, total_time, rmsdiv, ke, cfl, tau_bot) every `every` steps."""
+        self._check(self._lib.lesgo_gpu_diag_log_config(self._h, every, capacity))
+
+    def diag_log_sample(self):
+        self._check(self._lib.lesgo_gpu_diag_log_sample(self._h))
+
+    def diag_log(self, maxrows: int = 65536) -> np.ndarray:
+        out = np.zeros((maxrows, 6))
+        n = C.c_int()
+        self._check(self._lib.lesgo_gpu_diag_log_read(self._h, -1, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                      maxrows, C.byref(n)))
+        return out[:n.value].copy()
+
     # ---------------- time averaging ---------------------------------------------------
     def tavg_config(self, nstart: int, nend: int, nskip: int):
         """tavg_nstart / tavg_nend / tavg_nskip of the reference's input."""
@@ -462,6 +477,21 @@ class LesgoBatch:
 
     def launches_per_step(self, with_sgs_update: bool = False) -> int:
         return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
+
+    # ---------------- diagnostics log ---------------------------------------------------
+    def diag_log_config(self, every: int, capacity: int = 1024):
+        """Rows of (jt_total, total_time, rmsdiv, ke, cfl, tau_bot) every `every` steps."""
+        self._check(self._lib.lesgo_gpu_diag_log_config(self._h, every, capacity))
+
+    def diag_log_sample(self):
+        self._check(self._lib.lesgo_gpu_diag_log_sample(self._h))
+
+    def diag_log(self, iid: int, maxrows: int = 65536) -> np.ndarray:
+        out = np.zeros((maxrows, 6))
+        n = C.c_int()
+        self._check(self._lib.lesgo_gpu_diag_log_read(self._h, iid, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                      maxrows, C.byref(n)))
+        return out[:n.value].copy()
 
     # ---------------- time averaging ---------------------------------------------------
     def tavg_config(self, nstart: int, nend: int, nskip: int):
