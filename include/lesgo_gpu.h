@@ -325,6 +325,16 @@ int lesgo_gpu_sim_time(lesgo_handle_t* h, int id, double* total_time);
  * chose on the device; before the first step the input dt). */
 int lesgo_gpu_time_step(lesgo_handle_t* h, int id, double* dt);
 
+/* ---- tile-shape autotuner (no reference counterpart) ----------------------
+ * Picks the tile shapes of the transform passes (complex values per block of
+ * the x passes, shared-memory bytes per block of the y passes) by timing the
+ * handle's own fused step at every candidate, and returns them.  The fields,
+ * step constants and disk states are copied aside on the device first and
+ * put back after, so the simulation state is unchanged (tile shapes do not
+ * change results); without memory for that copy the passes are timed alone
+ * on scratch buffers.  Call it once after the instances are in place. */
+int lesgo_gpu_autotune(lesgo_handle_t* h, int* xtarget, int* ybudget);
+
 /* ---- instrumentation (no reference counterpart; the reference only
  * prints wall-clock times, main.f90:359-436) --------------------------- */
 /* enable != 0: run steps eagerly (no graph replay) with a CUDA event pair

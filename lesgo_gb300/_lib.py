@@ -115,6 +115,7 @@ SIGNATURES = {
     "lesgo_gpu_counters_inst": (_I, [_H, _I, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_turbine_state_inst": (_I, [_H, _I, _D, _D, _D, _I]),
     "lesgo_gpu_footprint": (_I, [C.POINTER(Params), _I, C.POINTER(C.c_longlong)]),
+    "lesgo_gpu_autotune": (_I, [_H, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_diag_log_config": (_I, [_H, _I, _I]),
     "lesgo_gpu_diag_log_sample": (_I, [_H]),
     "lesgo_gpu_diag_log_read": (_I, [_H, _I, _D, _I, C.POINTER(_I)]),

@@ -397,8 +397,7 @@ __global__ void k_interp(InterpArgs<R> a) {
 // input in the reference's order: u_j = (r_j - a_j u_{j-1}) / bet_j forward,
 // u_j = u_j - gam_{j+1} u_{j+1} backward.
 // ---------------------------------------------------------------------------
-constexpr int kThomasSeg = 8;     // segments per column
-constexpr int kThomasCols = 32;   // columns per block (one warp per segment row)
+// SEG segments per column, COLS columns per block (SEG * COLS = 256 threads).
 
 struct ThomasArgs {
   const double2 *Hx, *Hy, *Hz;   // levels 1..nz at index level-1, [inst][nz][P]
@@ -424,12 +423,13 @@ __device__ __forceinline__ double2 thomas_rhs(const ThomasArgs& a, const double2
                       (hx.x * kxv) + (hy.x * kyv) + (hz.y - hzp.y) * c4);
 }
 
-__global__ void __launch_bounds__(kThomasCols * kThomasSeg) k_thomas(ThomasArgs a) {
-  __shared__ double2 s_x[kThomasSeg][kThomasCols];   // segment end value / start value
-  __shared__ double s_h[kThomasSeg][kThomasCols];    // segment map slope
-  const int lane = threadIdx.x % kThomasCols, seg = threadIdx.x / kThomasCols;
+template <int SEG, int COLS>
+__global__ void __launch_bounds__(SEG * COLS) k_thomas(ThomasArgs a) {
+  __shared__ double2 s_x[SEG][COLS];   // segment end value / start value
+  __shared__ double s_h[SEG][COLS];    // segment map slope
+  const int lane = threadIdx.x % COLS, seg = threadIdx.x / COLS;
   const long long P = (long long)a.ny * a.K;
-  const long long gcol = (long long)blockIdx.x * kThomasCols + lane;
+  const long long gcol = (long long)blockIdx.x * COLS + lane;
   const bool live = gcol < P * a.ninst;
   const int inst = live ? (int)(gcol / P) : 0;
   const int t = live ? (int)(gcol - inst * P) : 0;
@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(kThomasCols * kThomasSeg) k_thomas(ThomasArgs 
   double2* phat = a.phat + (long long)inst * (nz + 1) * P;   // u_j at phat[(j-1)*P]
   const bool nyq = jy == a.ny / 2;
   const bool mean = kx == 0 && jy == 0;
-  const int L = (n + kThomasSeg - 1) / kThomasSeg;
+  const int L = (n + SEG - 1) / SEG;
   const int j0 = 1 + seg * L, j1 = min(n, j0 + L - 1);   // this thread's levels (may be empty)
   const double c3 = 1.0 / (a.dz * a.dz);
   const double kxv = a.kxw[kx], kyv = a.kyw[jy];
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(kThomasCols * kThomasSeg) k_thomas(ThomasArgs 
   s_h[seg][lane] = g;
   __syncthreads();
   double2 y = make_double2(0.0, 0.0);   // v_{j1+1}; the top segment has none
-  for (int s = kThomasSeg - 1; s > seg; --s) {
+  for (int s = SEG - 1; s > seg; --s) {
     const double2 e = s_x[s][lane];
     const double gs = s_h[s][lane];
     y = make_double2(e.x + gs * y.x, e.y + gs * y.y);

@@ -361,6 +361,7 @@ class SolverBase {
   virtual double sim_time(int id) = 0;
   virtual double time_step(int id) = 0;
   virtual void diag_log_config(int every, int capacity) = 0;
+  virtual void autotune(int* xtarget, int* ybudget) = 0;
   virtual void diag_log_sample() = 0;
   virtual int diag_log_read(int id, double* out, int maxrows) = 0;
 };
@@ -375,6 +376,7 @@ static long long footprint_bytes(const Derived& d, int cap) {
   b += (LESGO_NFIELDS + 4 + (d.turbines.empty() ? 0 : 1)) * nf * rs;   // fields, interpolation temps, fza on uv
   b += 4 * plane * rs + 6 * (long long)(d.nz + 1) * pbig * rs;          // wall planes, 3/2-grid fields
   b += (std::max({21 * vs, 6 * vs, 3 * vb}) + std::max({42 * vs, 6 * vb, 9 * vs}) + 4 * ps) * 2 * rs;   // spectra
+  b += (std::max(6 * vs, 3 * vb) + std::max(6 * vb, 3 * vs)) * 2 * rs;                             // convec spectra
   b += (3 * vs + 2 * ps + (long long)(d.nz + 1) * ps) * 16;                                          // FP64 pressure
   return b * cap + 2LL * (d.nz + 2) * ps * 8;                                                       // Thomas pivots
 }
@@ -414,6 +416,12 @@ class Solver : public SolverBase {
     specA_ = alloc<T2>(std::max({21 * vol1_s_, 6 * vol1_s_, 3 * vol1_b_}) * cap_);
     specB_ = alloc<T2>(std::max({42 * vol1_s_, 6 * vol1_b_, 9 * vol1_s_}) * cap_);
     specC_ = alloc<T2>(4LL * pl_s * cap_);
+    // the convective term's own spectra: it runs beside the stress
+    // divergence (and the Lagrangian update) in the fused step
+    cvA_ = alloc<T2>(std::max(6 * vol1_s_, 3 * vol1_b_) * cap_);
+    cvB_ = alloc<T2>(std::max(6 * vol1_b_, 3 * vol1_s_) * cap_);
+    CK(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+    for (auto& e : ev_) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     hspec_ = alloc<double2>(3 * vol1_s_ * cap_);
     hplane_ = alloc<double2>(2 * pl_s * cap_);
     phat_ = alloc<double2>((nz + 1) * pl_s * cap_);
@@ -429,6 +437,8 @@ class Solver : public SolverBase {
     kp_.sc = sc_d_;
     // LESGO_GRAPHS=0 replays nothing: every step launches eagerly
     if (const char* g = std::getenv("LESGO_GRAPHS")) graphs_allowed_ = std::strcmp(g, "0") != 0;
+    if (const char* e = std::getenv("LESGO_XTARGET")) xtarget_ = std::max(256, std::atoi(e));
+    if (const char* e = std::getenv("LESGO_YBUDGET")) ybudget_ = (size_t)std::max(8192, std::atoi(e));
     use_graphs_ = graphs_allowed_;
     build_tables();
     CK(cudaStreamSynchronize(st_));
@@ -439,6 +449,9 @@ class Solver : public SolverBase {
     for (auto& r : prof_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
     for (void* p : allocs_) cudaFree(p);
+    for (auto& e : ev_)
+      if (e) cudaEventDestroy(e);
+    if (st2_) cudaStreamDestroy(st2_);
     if (st_) cudaStreamDestroy(st_);
   }
 
@@ -1024,6 +1037,121 @@ class Solver : public SolverBase {
     out[3] = std::sqrt((h[5] / nxy) * (h[5] / nxy) + (h[6] / nxy) * (h[6] / nxy));
   }
 
+  // ---------------- tile-shape autotuner ----------------------------------------
+  // Picks the tile shapes of the transform passes (complex values per block
+  // of the x passes, shared memory per block of the y passes) by timing this
+  // handle's own fused step at every candidate: the fields, step constants
+  // and disk states are copied aside, a normal step, a second normal step and
+  // a step with the dynamic update run eagerly per candidate, and the copy is
+  // put back, so the simulation state is unchanged (tile shapes do not change
+  // results).  Without memory for the copy, the passes are timed alone on
+  // scratch buffers instead.
+  void autotune(int* xt_out, int* yb_out) override {
+    need_active();
+    const size_t fbytes = (size_t)nfield_ * sizeof(R);
+    const size_t sbytes = (size_t)SC_N * cap_ * sizeof(double);
+    const size_t tbytes = kp_.turbines ? 3 * (size_t)th_.n * sizeof(double) : 0;
+    unsigned char* snap = nullptr;
+    if (cudaMalloc(&snap, fbytes * LESGO_NFIELDS + sbytes + tbytes) != cudaSuccess) {
+      cudaGetLastError();
+      autotune_passes();
+    } else {
+      auto save = [&](bool back) {
+        unsigned char* q = snap;
+        auto mv = [&](void* dev, size_t n) {
+          CK(cudaMemcpyAsync(back ? dev : (void*)q, back ? (const void*)q : dev, n, cudaMemcpyDeviceToDevice, st_));
+          q += n;
+        };
+        for (int f = 0; f < LESGO_NFIELDS; ++f) mv(F_[f], fbytes);
+        mv(sc_d_, sbytes);
+        if (tbytes) { mv(td_.u_d, tbytes / 3); mv(td_.u_d_T, tbytes / 3); mv(td_.f_n, tbytes / 3); }
+      };
+      save(false);
+      cudaEvent_t e0, e1;
+      CK(cudaEventCreate(&e0));
+      CK(cudaEventCreate(&e1));
+      float best = 1e30f;
+      int bx = xtarget_;
+      size_t by = ybudget_;
+      for (int xt : {1024, 2048, 4096})
+        for (size_t yb : {(size_t)32768, (size_t)49152, (size_t)65536, (size_t)112640}) {
+          xtarget_ = xt;
+          ybudget_ = yb;
+          step_body(false);   // sets the kernels' shared-memory limits at this shape
+          CK(cudaEventRecord(e0, st_));
+          step_body(false);
+          step_body(false);
+          step_body(true);
+          CK(cudaEventRecord(e1, st_));
+          CK(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          CK(cudaEventElapsedTime(&ms, e0, e1));
+          if (ms < best) { best = ms; bx = xt; by = yb; }
+        }
+      xtarget_ = bx;
+      ybudget_ = by;
+      save(true);
+      CK(cudaStreamSynchronize(st_));
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      cudaFree(snap);
+    }
+    graphs_clear();   // tile shapes are part of the captured launches
+    if (xt_out) *xt_out = xtarget_;
+    if (yb_out) *yb_out = (int)ybudget_;
+  }
+  // The fallback: the three pass kinds timed alone on scratch buffers (6
+  // fields forward from the fields and inverse into the 3/2-grid scratch;
+  // 1 -> 3 and 5 -> 3 y passes on scratch spectra).
+  void autotune_passes() {
+    const int nz = d_.nz, ny = d_.ny;
+    const InstMap im = imf(nz);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto timed = [&](auto&& fn) {
+      fn();
+      CK(cudaEventRecord(e0, st_));
+      for (int r = 0; r < 3; ++r) fn();
+      CK(cudaEventRecord(e1, st_));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      return ms;
+    };
+    const R sc = (R)(1.0 / ((double)d_.nx * ny));
+    float best = 1e30f;
+    int best_x = xtarget_;
+    for (int xt : {1024, 2048, 4096}) {
+      xtarget_ = xt;
+      const float ms = timed([&] {
+        SrcFields<R, 6> src{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDX], F_[LESGO_DUDY], F_[LESGO_DUDZ]},
+                            sc, 1, 1, d_.ld, kp_.plane, im};
+        xfwd<6>(src, d_.nx, ny, nz, specA_, px_, "tune.xfwd");
+        DstFields<R, 6> dst{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld, kp_.plane, im};
+        xinv<6>(dst, specA_, d_.nx, ny, nz, px_, "tune.xinv");
+      });
+      if (ms < best) { best = ms; best_x = xt; }
+    }
+    xtarget_ = best_x;
+    best = 1e30f;
+    size_t best_y = ybudget_;
+    for (size_t yb : {(size_t)32768, (size_t)49152, (size_t)65536, (size_t)112640}) {
+      ybudget_ = yb;
+      const float ms = timed([&] {
+        ypass_lin<1, 3, true, true, T2, T2>(specA_, 0, 1, nz, ny, specB_, ny, nz, 3, ROW_SAME,
+                                            {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}}, "tune.ypass13");
+        ypass_lin<5, 3, true, true, T2, T2>(specA_, 0, 1, nz, ny, specB_, ny, nz, 1, ROW_SAME,
+                                            {{MUL_IKX, MUL_IKY}, {MUL_ZERO, MUL_IKX, MUL_IKY}, {MUL_ZERO, MUL_ZERO,
+                                             MUL_ZERO, MUL_IKX, MUL_IKY}}, "tune.ypass53");
+      });
+      if (ms < best) { best = ms; best_y = yb; }
+    }
+    ybudget_ = best_y;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+
   // ---------------- diagnostics log (main.f90:359-436: wbase / nenergy) -----
   void diag_log_config(int every, int capacity) override {
     if (every < 1 || capacity < 1) throw Error(LESGO_ERR_ARG, "diag log: every and capacity must be >= 1");
@@ -1354,20 +1482,28 @@ class Solver : public SolverBase {
     DstFields<R, 9> dst{{F_[LESGO_U], F_[LESGO_DUDX], F_[LESGO_DUDY], F_[LESGO_V], F_[LESGO_DVDX], F_[LESGO_DVDY],
                          F_[LESGO_W], F_[LESGO_DWDX], F_[LESGO_DWDY]}, 1, 1, d_.ld, kp_.plane, im};
     xinv<9>(dst, specB_, d_.nx, d_.ny, d_.nz, px_, "filt_da.xinv");
-    // wall model inputs (test-filtered first level), main.f90:180-189
+    // Two branches from here.  Branch: the applied forcing (filtered velocity
+    // of this step, main.f90:248-257), then, once the column pass is done,
+    // the dynamic update and the stress divergence.  Main: the wall-model
+    // inputs (main.f90:180-189), sgs_stag with ddz and the wall values fused
+    // (main.f90:164-189), the convective term.  They meet before the RHS
+    // epilogue, which reads all of them.
+    fork(0);
+    if (kp_.turbines) on_branch([&] { turb_impl(); });
     wall_planes();
-    // applied forcing uses the filtered velocity of this step (main.f90:248-257)
-    if (kp_.turbines) turb_impl();
-    // sgs_stag with ddz_uv/ddz_w and the wall values fused (main.f90:164-189)
-    if (!lag_any) {
-      column<COL_DDZ | COL_TAU>();
-    } else {
-      column<COL_DDZ | COL_STORE_S>();
-      lagrange();
-      column<COL_READ_S | COL_TAU>();
-    }
-    divstress(3);
-    convec_impl(true);
+    if (!lag_any) column<COL_DDZ | COL_TAU>();
+    else column<COL_DDZ | COL_STORE_S>();
+    fork(1);
+    on_branch([&] {
+      if (lag_any) {
+        lagrange();
+        column<COL_READ_S | COL_TAU>();
+      }
+      divstress(3);
+    });
+    convec_part1();
+    join(2);
+    convec_part2(true);
     pressure_impl(true);
   }
 
@@ -1552,7 +1688,7 @@ class Solver : public SolverBase {
             int in_fields = NF) {
     XfGeom g;
     g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nli * kp_.ninst; g.ls = M / 2 + 1;
-    const int target = sizeof(R) == 8 ? 2048 : 4096;
+    const int target = xtarget_;
     g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
     g.out_field_stride = (long long)g.nrows * g.K;
     g.fH = FastDiv((unsigned)(M / 2)); g.fK = FastDiv((unsigned)g.K);
@@ -1570,7 +1706,7 @@ class Solver : public SolverBase {
             int out_fields = NF) {
     XiGeom g;
     g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nli * kp_.ninst; g.ls = M / 2 + 1;
-    const int target = sizeof(R) == 8 ? 2048 : 4096;
+    const int target = xtarget_;
     g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
     g.in_field_stride = (long long)g.nrows * g.K;
     g.fH = FastDiv((unsigned)(M / 2)); g.fM = FastDiv((unsigned)M);
@@ -1611,7 +1747,7 @@ class Solver : public SolverBase {
     g.ls_in = in_rows + 1; g.ls_out = out_rows + 1;
     const FftPlan<R>& pin = (in_rows == d_.ny) ? py_ : pyb_;
     const FftPlan<R>& pout = (out_rows == d_.ny) ? py_ : pyb_;
-    const size_t budget = 110 * 1024;
+    const size_t budget = ybudget_;
     int tk = sizeof(R) == 8 ? 8 : 16;
     auto smem_of = [&](int t) {
       const size_t s = (size_t)NIN * t * g.ls_in;
@@ -1712,27 +1848,37 @@ class Solver : public SolverBase {
     xinv<42>(dst, specB_, d_.nx, d_.ny, d_.nz, px_, "lagrange.xinv", 13);
   }
 
+  // convec.f90:21-333: vorticity and velocity to the 3/2 grid, the three
+  // products there, back to the kept modes (part 1); the RHS epilogue, with
+  // the AB2 advance when fused (part 2).
   void convec_impl(bool fused) {
+    convec_part1();
+    convec_part2(fused);
+  }
+  void convec_part1() {
     const R c = (R)(1.0 / ((double)d_.nx * d_.ny));
     const InstMap im = imf(d_.nz);
     const InstMap imb(d_.nz, kp_.istride_big);
     SrcVort<R> sv{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDY], F_[LESGO_DUDZ], F_[LESGO_DVDX],
                   F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane, im};
-    xfwd<6>(sv, d_.nx, d_.ny, d_.nz, specA_, px_, "convec.xfwd", 9);
-    ypass_lin<1, 1, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}},
+    xfwd<6>(sv, d_.nx, d_.ny, d_.nz, cvA_, px_, "convec.xfwd", 9);
+    ypass_lin<1, 1, true, true, T2, T2>(cvA_, 0, 1, d_.nz, d_.ny, cvB_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}},
                                         "convec.ypass_pad");
     DstFields<R, 6> db{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld_big, kp_.plane_big, imb};
-    xinv<6>(db, specB_, d_.nx2, d_.ny2, d_.nz, pxb_, "convec.xinv_big");
+    xinv<6>(db, cvB_, d_.nx2, d_.ny2, d_.nz, pxb_, "convec.xinv_big");
     const R cb = (R)(1.0 / ((double)d_.nx2 * d_.ny2));
     SrcConvProd<R> sp{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5], cb, d_.ld_big, d_.nz, kp_.plane_big, imb};
-    xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, specA_, pxb_, "convec.xfwd_big", 6);
-    ypass_lin<1, 1, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny2, specB_, d_.ny, d_.nz, 3, ROW_UNPAD, {{MUL_ONE}},
+    xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, cvA_, pxb_, "convec.xfwd_big", 6);
+    ypass_lin<1, 1, true, true, T2, T2>(cvA_, 0, 1, d_.nz, d_.ny2, cvB_, d_.ny, d_.nz, 3, ROW_UNPAD, {{MUL_ONE}},
                                         "convec.ypass_unpad");
+  }
+  void convec_part2(bool fused) {
+    const InstMap im = imf(d_.nz);
     if (!fused) {
       DstConvec<R, false> dc{};
       dc.RHSx = F_[LESGO_RHSX]; dc.RHSy = F_[LESGO_RHSY]; dc.RHSz = F_[LESGO_RHSZ];
       dc.ld = d_.ld; dc.nz = d_.nz; dc.plane = kp_.plane; dc.iflags = flags_d_; dc.im = im;
-      xinv<3>(dc, specB_, d_.nx, d_.ny, d_.nz, px_);
+      xinv<3>(dc, cvB_, d_.nx, d_.ny, d_.nz, px_);
     } else {
       DstConvec<R, true> dc{};
       dc.RHSx = F_[LESGO_RHSX]; dc.RHSy = F_[LESGO_RHSY]; dc.RHSz = F_[LESGO_RHSZ];
@@ -1743,8 +1889,31 @@ class Solver : public SolverBase {
       dc.sc = sc_d_; dc.mpfx = d_.mpfx; dc.mpfy = d_.mpfy;
       dc.ld = d_.ld; dc.nz = d_.nz; dc.use_mpf = d_.p.use_mean_p_force; dc.turbines = kp_.turbines;
       dc.iflags = flags_d_; dc.plane = kp_.plane; dc.im = im;
-      xinv<3>(dc, specB_, d_.nx, d_.ny, d_.nz, px_, "convec.xinv_ab2", 18 + 3 * kp_.turbines);
+      xinv<3>(dc, cvB_, d_.nx, d_.ny, d_.nz, px_, "convec.xinv_ab2", 18 + 3 * kp_.turbines);
     }
+  }
+
+  // Fork: work launched between fork() and join() with on_branch = true runs
+  // on the second stream once the main stream has reached the fork; join()
+  // makes the main stream wait for the branch.  Both are graph-capturable.
+  void fork(int e) {
+    CK(cudaEventRecord(ev_[e], st_));
+    CK(cudaStreamWaitEvent(st2_, ev_[e], 0));
+  }
+  void join(int e) {
+    CK(cudaEventRecord(ev_[e], st2_));
+    CK(cudaStreamWaitEvent(st_, ev_[e], 0));
+  }
+  template <class F>
+  void on_branch(F&& fn) {
+    std::swap(st_, st2_);
+    try {
+      fn();
+    } catch (...) {
+      std::swap(st_, st2_);
+      throw;
+    }
+    std::swap(st_, st2_);
   }
 
   void pressure_impl(bool fused) {
@@ -1754,12 +1923,17 @@ class Solver : public SolverBase {
     // scale 1/(nx ny tadv1 dt), the instance's step constant SC_PS
     SrcFields<R, 3> su{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, (R)0, 1, 1, d_.ld, kp_.plane, imf(nz), sc_d_, SC_PS};
     xfwd<3>(su, d_.nx, ny, nz, specA_, px_, "press.xfwd");
-    SrcFields<R, 1> sd{{F_[LESGO_DIVTZ]}, (R)c1, 1, nz - 1, d_.ld, kp_.plane, imf(2)};
-    xfwd<1>(sd, d_.nx, ny, 2, specC_, px_, "press.xfwd_bc");
+    // the boundary planes (divtz at levels 1 and nz) on the second stream
+    fork(3);
+    on_branch([&] {
+      SrcFields<R, 1> sd{{F_[LESGO_DIVTZ]}, (R)c1, 1, nz - 1, d_.ld, kp_.plane, imf(2)};
+      xfwd<1>(sd, d_.nx, ny, 2, specC_, px_, "press.xfwd_bc");
+      ypass_lin<1, 1, true, false, T2, double2>(specC_, 0, 1, 2, ny, hplane_, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
+                                                "press.ypass_fwd_bc");
+    });
     ypass_lin<1, 1, true, false, T2, double2>(specA_, 0, 1, nz, ny, hspec_, ny, nz, 3, ROW_SAME, {{MUL_ONE}},
                                               "press.ypass_fwd");
-    ypass_lin<1, 1, true, false, T2, double2>(specC_, 0, 1, 2, ny, hplane_, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
-                                              "press.ypass_fwd_bc");
+    join(4);
     const long long vs = vol1_s_ * kp_.ninst;
     ThomasArgs ta;
     ta.Hx = hspec_; ta.Hy = hspec_ + vs; ta.Hz = hspec_ + 2 * vs;
@@ -1768,13 +1942,24 @@ class Solver : public SolverBase {
     ta.kxw = kxw64_; ta.kyw = kyw64_;
     ta.dz = d_.dz; ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.ninst = kp_.ninst;
     pre();
-    k_thomas<<<(unsigned)((pl_s * kp_.ninst + kThomasCols - 1) / kThomasCols), kThomasCols * kThomasSeg, 0, st_>>>(ta);
+    // 16 segments per column when 8 would leave most SMs idle
+    const long long ncol = pl_s * kp_.ninst;
+    if (ncol * 8 < 152LL * 1024)
+      k_thomas<16, 16><<<(unsigned)((ncol + 15) / 16), 256, 0, st_>>>(ta);
+    else
+      k_thomas<8, 32><<<(unsigned)((ncol + 31) / 32), 256, 0, st_>>>(ta);
     post("press.thomas", (double)pl_s * kp_.ninst * (4.0 * nz + 1.0) * sizeof(double2));
     // p, i kx p, i ky p at levels 1..nz-1; p at levels 0 and nz (phat holds nz+1 planes per instance)
+    // p at levels 0 and nz on the second stream
+    fork(5);
+    on_branch([&] {
+      ypass_lin<1, 1, false, true, double2, T2>(phat_, 0, nz, nz + 1, ny, specC_, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
+                                                "press.ypass_inv_bc");
+      DstFields<R, 1> d0{{F_[LESGO_P]}, 0, nz, d_.ld, kp_.plane, imf(2)};
+      xinv<1>(d0, specC_, d_.nx, ny, 2, px_, "press.xinv_bc");
+    });
     ypass_lin<1, 3, false, true, double2, T2>(phat_, 1, 1, nz + 1, ny, specB_, ny, nz - 1, 1, ROW_SAME,
                                               {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}}, "press.ypass_inv");
-    ypass_lin<1, 1, false, true, double2, T2>(phat_, 0, nz, nz + 1, ny, specC_, ny, 2, 1, ROW_SAME, {{MUL_ONE}},
-                                              "press.ypass_inv_bc");
     if (fused) {
       DstPress<R, true> dp{F_[LESGO_P], F_[LESGO_DPDX], F_[LESGO_DPDY], F_[LESGO_RHSX], F_[LESGO_RHSY], F_[LESGO_U],
                            F_[LESGO_V], sc_d_, d_.ld, kp_.plane, imf(nz - 1)};
@@ -1784,8 +1969,7 @@ class Solver : public SolverBase {
                             F_[LESGO_V], sc_d_, d_.ld, kp_.plane, imf(nz - 1)};
       xinv<3>(dp, specB_, d_.nx, ny, nz - 1, px_);
     }
-    DstFields<R, 1> d0{{F_[LESGO_P]}, 0, nz, d_.ld, kp_.plane, imf(2)};
-    xinv<1>(d0, specC_, d_.nx, ny, 2, px_, "press.xinv_bc");
+    join(6);
     const long long n = (long long)d_.nx * ny * nz * kp_.ninst;
     pre();
     if (fused)
@@ -1830,9 +2014,16 @@ class Solver : public SolverBase {
   double *ibet_ = nullptr, *tgam_ = nullptr;
   double *tacc_ = nullptr, *tw_d_ = nullptr, *prof_d_ = nullptr;
   double* sc_d_ = nullptr;                   // step constants [cap][SC_N]
+  T2 *cvA_ = nullptr, *cvB_ = nullptr;       // convective-term spectra
+  cudaStream_t st2_ = nullptr;               // second branch of the fused step
+  cudaEvent_t ev_[8] = {};
   unsigned long long* cflmax_d_ = nullptr;   // per-instance |u|, |v|, |w| maxima
   int* tact_d_ = nullptr;                    // time-averaging action per instance
   double* dlog_ = nullptr;                   // diagnostics log [cap][dlog_cap_][6]
+  // tile shapes: complex values per block of the x passes, shared-memory
+  // bytes per block of the y passes
+  int xtarget_ = 2048;
+  size_t ybudget_ = sizeof(R) == 8 ? 110 * 1024 : 48 * 1024;
   int dlog_cap_ = 0, dlog_every_ = 0;
   long long tacc_stride_ = 0;
   bool tavg_on_ = false;
@@ -2365,3 +2556,7 @@ int lesgo_gpu_diag_log_read(lesgo_handle_t* h, int id, double* rows, int maxrows
   return guarded(h, [&] { *nrows = h->s->diag_log_read(id < 0 ? h->inst0 : id, rows, maxrows); });
 }
 }  // extern "C"
+
+extern "C" int lesgo_gpu_autotune(lesgo_handle_t* h, int* xtarget, int* ybudget) {
+  return guarded(h, [&] { h->s->autotune(xtarget, ybudget); });
+}

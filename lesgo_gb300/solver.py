@@ -310,6 +310,12 @@ class LesgoGPU:
     def launches_per_step(self, with_sgs_update: bool = False) -> int:
         return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
 
+    def autotune(self) -> Dict[str, int]:
+        """Pick the transform tile shapes for this grid by timing them."""
+        xt, yb = C.c_int(), C.c_int()
+        self._check(self._lib.lesgo_gpu_autotune(self._h, C.byref(xt), C.byref(yb)))
+        return dict(xtarget=xt.value, ybudget=yb.value)
+
     # ---------------- diagnostics log ---------------------------------------------------
     def diag_log_config(self, every: int, capacity: int = 1024):
         """Rows of (jt_total, total_time, rmsdiv, ke, cfl, tau_bot) every `every` steps."""
@@ -432,6 +438,13 @@ class LesgoBatch:
         self._check(self._lib.lesgo_gpu_get_field_inst(self._h, iid, LesgoGPU._fid(name), out.ctypes.data, lbz, nzhi))
         return out
 
+    def set_ptr(self, iid: int, name, ptr: int, lbz: int, nzhi: int):
+        """Copy levels lbz..nzhi of instance iid from a host FP64 buffer at ``ptr``."""
+        self._check(self._lib.lesgo_gpu_set_field_inst(self._h, iid, LesgoGPU._fid(name), C.c_void_p(ptr), lbz, nzhi))
+
+    def get_ptr(self, iid: int, name, ptr: int, lbz: int, nzhi: int):
+        self._check(self._lib.lesgo_gpu_get_field_inst(self._h, iid, LesgoGPU._fid(name), C.c_void_p(ptr), lbz, nzhi))
+
     def set(self, iid: int, name, arr: np.ndarray, lbz: int = 0):
         a = np.ascontiguousarray(arr, dtype=np.float64)
         self._check(self._lib.lesgo_gpu_set_field_inst(self._h, iid, LesgoGPU._fid(name), a.ctypes.data, lbz,
@@ -477,6 +490,12 @@ class LesgoBatch:
 
     def launches_per_step(self, with_sgs_update: bool = False) -> int:
         return self._lib.lesgo_gpu_launches_per_step(self._h, 1 if with_sgs_update else 0)
+
+    def autotune(self) -> Dict[str, int]:
+        """Pick the transform tile shapes for this grid by timing them."""
+        xt, yb = C.c_int(), C.c_int()
+        self._check(self._lib.lesgo_gpu_autotune(self._h, C.byref(xt), C.byref(yb)))
+        return dict(xtarget=xt.value, ybudget=yb.value)
 
     # ---------------- diagnostics log ---------------------------------------------------
     def diag_log_config(self, every: int, capacity: int = 1024):

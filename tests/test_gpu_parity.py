@@ -196,3 +196,19 @@ def test_batch_alone_equals_mixed(built_lib):
             assert b.counters(iid) == g.counters()
             g.close()
         b.close()
+
+
+@pytest.mark.parametrize("grid", [(32, 32, 16), (256, 192, 8)])
+def test_pressure_solve_both_segmentations(built_lib, grid):
+    """The Thomas solve runs 16 segments per column on small column counts
+    and 8 on large ones (here 256x192: 24576 columns); both against the
+    oracle after 2 steps."""
+    nx, ny, Nz = grid
+    p, o, g = make_pair(nx=nx, ny=ny, Nz=Nz, dyn_init=100)
+    for _ in range(2):
+        o.step()
+    g.step(2)
+    for f in ("p", "u", "w"):
+        e = rel_err(p, f, g.get(f), oracle_field(o, f))
+        assert e < 1e-11, (grid, f, e)
+    g.close()
