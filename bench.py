@@ -66,6 +66,8 @@ def parse():
                     "B = 128^3 half channel, C = 256x256x192 wind farm with 12 actuator disks")
     ap.add_argument("--val-steps", type=int, default=None)
     ap.add_argument("--val-window", type=int, default=2000)
+    ap.add_argument("--only-class", default=None, help="run only the ensemble's instances of one grid class, "
+                    "e.g. 96x96x64 (each class is an independent batch: used to profile its launches alone)")
     return ap.parse_args()
 
 
@@ -179,7 +181,7 @@ BATCH_GRIDS = [(48, 48, 48), (64, 64, 64), (96, 96, 64), (128, 64, 64)]
 
 def batch_instances(n=48, seed=2024):
     """The 48-instance ensemble: grid drawn from BATCH_GRIDS, z0 log-uniform
-    in [1e-5, 1e-3], own IC seed."""
+    in [1e-5, 1e-3], own IC seed (restricted to one class with --only-class)."""
     import math
     import numpy as np
     rng = np.random.default_rng(seed)
@@ -188,7 +190,14 @@ def batch_instances(n=48, seed=2024):
         g = BATCH_GRIDS[int(rng.integers(len(BATCH_GRIDS)))]
         zo = math.exp(rng.uniform(math.log(1e-5), math.log(1e-3)))
         out.append((g, zo, 5000 + i))
+    if ONLY_CLASS:
+        out = [x for x in out if "x".join(map(str, x[0])) == ONLY_CLASS]
+        if not out:
+            raise SystemExit(f"no instance of class {ONLY_CLASS}")
     return out
+
+
+ONLY_CLASS = None
 
 
 def make_batches(precision="mixed"):
@@ -599,7 +608,9 @@ def run_validate(args):
 
 
 def main():
+    global ONLY_CLASS
     args = parse()
+    ONLY_CLASS = args.only_class
     if args.impl == "reference":
         run_reference(args)
     elif args.validate:

@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src
   T2* B = A + nl * g.ls;
   const int H = g.M / 2;
   const int row0 = blockIdx.x * g.rpc;
+  #pragma unroll 4
   for (int t = threadIdx.x; t < g.rpc * H; t += blockDim.x) {
     const int r = g.fH.div(t), nn = t - r * H;
     const int row = row0 + r;
@@ -253,6 +254,7 @@ __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src
   __syncthreads();
   T2* Z = fft_lines<R, false>(A, B, nl, g.ls, plan);
   const R half = (R)0.5;
+  #pragma unroll 4
   for (int t = threadIdx.x; t < nl * g.K; t += blockDim.x) {
     const int l = g.fK.div(t), kk = t - l * g.K;
     const int f = g.frpc.div(l), r = l - f * g.rpc;
@@ -292,6 +294,7 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
   T2* B = A + nl * g.ls;
   const int row0 = blockIdx.x * g.rpc;
   // build Z[k] = (X[k] + conj X[H-k]) + i W^-k (X[k] - conj X[H-k])
+  #pragma unroll 4
   for (int t = threadIdx.x; t < nl * H; t += blockDim.x) {
     const int l = g.fH.div(t), k = t - l * H;
     const int f = g.frpc.div(l), r = l - f * g.rpc;
@@ -313,6 +316,7 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
   __syncthreads();
   T2* Z = fft_lines<R, true>(A, B, nl, g.ls, plan);
   const R* Zr = reinterpret_cast<const R*>(Z);
+  #pragma unroll 4
   for (int t = threadIdx.x; t < g.rpc * g.M; t += blockDim.x) {
     const int r = g.fM.div(t), i = t - r * g.M;
     const int row = row0 + r;
@@ -358,6 +362,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
   const int grp = blockIdx.z;
   const int tk = min(g.tk, g.K - kx0);
   // load inputs: element (jy, c) of input i
+  #pragma unroll 4
   for (int t = threadIdx.x; t < NIN * g.ny_in * g.tk; t += blockDim.x) {
     const int c = t & (g.tk - 1);
     const int rest = t >> g.tk_log2;
@@ -396,6 +401,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
     __syncthreads();
     T2* res = W0;
     if (INV) res = fft_lines<R, true>(W0, W1, g.tk, g.ls_out, pout);
+    #pragma unroll 4
     for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
       const int ky = t >> g.tk_log2, c = t & (g.tk - 1);
       if (c < tk) op.store(grp, o, li, ky, kx0 + c, res[c * g.ls_out + ky]);

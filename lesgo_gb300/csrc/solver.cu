@@ -437,6 +437,7 @@ class Solver : public SolverBase {
     kp_.sc = sc_d_;
     // LESGO_GRAPHS=0 replays nothing: every step launches eagerly
     if (const char* g = std::getenv("LESGO_GRAPHS")) graphs_allowed_ = std::strcmp(g, "0") != 0;
+    if (const char* b = std::getenv("LESGO_BRANCHES")) branches_allowed_ = std::strcmp(b, "0") != 0;
     if (const char* e = std::getenv("LESGO_XTARGET")) xtarget_ = std::max(256, std::atoi(e));
     if (const char* e = std::getenv("LESGO_YBUDGET")) ybudget_ = (size_t)std::max(8192, std::atoi(e));
     use_graphs_ = graphs_allowed_;
@@ -1896,16 +1897,25 @@ class Solver : public SolverBase {
   // Fork: work launched between fork() and join() with on_branch = true runs
   // on the second stream once the main stream has reached the fork; join()
   // makes the main stream wait for the branch.  Both are graph-capturable.
+  // While profiling (or with LESGO_BRANCHES=0, for external profilers),
+  // branches run on the main stream, so that each kernel is timed alone.
+  bool serial() const { return prof_on_ || !branches_allowed_; }
   void fork(int e) {
+    if (serial()) return;
     CK(cudaEventRecord(ev_[e], st_));
     CK(cudaStreamWaitEvent(st2_, ev_[e], 0));
   }
   void join(int e) {
+    if (serial()) return;
     CK(cudaEventRecord(ev_[e], st2_));
     CK(cudaStreamWaitEvent(st_, ev_[e], 0));
   }
   template <class F>
   void on_branch(F&& fn) {
+    if (serial()) {
+      fn();
+      return;
+    }
     std::swap(st_, st2_);
     try {
       fn();
@@ -2047,6 +2057,7 @@ class Solver : public SolverBase {
   bool use_graphs_ = true, graphs_allowed_ = true;
   int launches_ = 0;
   bool prof_on_ = false;
+  bool branches_allowed_ = true;   // LESGO_BRANCHES=0: the fused step on one stream
   cudaEvent_t prof_start_ = nullptr;
   std::vector<ProfRec> prof_;
   std::map<int, cudaGraphExec_t> graphs_;
