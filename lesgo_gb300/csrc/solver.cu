@@ -1477,8 +1477,9 @@ class Solver : public SolverBase {
     const InstMap im = imf(d_.nz);
     SrcFields<R, 3> src{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W]}, (R)(1.0 / ((double)d_.nx * d_.ny)), 1, 1, d_.ld,
                         kp_.plane, im};
-    xfwd<3>(src, d_.nx, d_.ny, d_.nz, specA_, px_, "filt_da.xfwd");
-    ypass_lin<1, 3, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 3, ROW_SAME,
+    // into the convective term's spectra, which reuses them (convec_part1)
+    xfwd<3>(src, d_.nx, d_.ny, d_.nz, cvA_, px_, "filt_da.xfwd");
+    ypass_lin<1, 3, true, true, T2, T2>(cvA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 3, ROW_SAME,
                                         {{MUL_ONE}, {MUL_IKX}, {MUL_IKY}}, "filt_da.ypass");
     DstFields<R, 9> dst{{F_[LESGO_U], F_[LESGO_DUDX], F_[LESGO_DUDY], F_[LESGO_V], F_[LESGO_DVDX], F_[LESGO_DVDY],
                          F_[LESGO_W], F_[LESGO_DWDX], F_[LESGO_DWDY]}, 1, 1, d_.ld, kp_.plane, im};
@@ -1502,7 +1503,7 @@ class Solver : public SolverBase {
       }
       divstress(3);
     });
-    convec_part1();
+    convec_part1(true);
     join(2);
     convec_part2(true);
     pressure_impl(true);
@@ -1853,16 +1854,27 @@ class Solver : public SolverBase {
   // products there, back to the kept modes (part 1); the RHS epilogue, with
   // the AB2 advance when fused (part 2).
   void convec_impl(bool fused) {
-    convec_part1();
+    convec_part1(false);
     convec_part2(fused);
   }
-  void convec_part1() {
+  // uvw_ready: the first three spectra of cvA_ already hold the x transforms
+  // of u, v, w (filt_da's forward pass in the fused step).  They are those of
+  // the field before filt_da's filter, which differs from the filtered field
+  // only in the ky = ny/2 row, and the 3/2 padding below drops that row.
+  void convec_part1(bool uvw_ready) {
     const R c = (R)(1.0 / ((double)d_.nx * d_.ny));
     const InstMap im = imf(d_.nz);
     const InstMap imb(d_.nz, kp_.istride_big);
-    SrcVort<R> sv{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDY], F_[LESGO_DUDZ], F_[LESGO_DVDX],
-                  F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane, im};
-    xfwd<6>(sv, d_.nx, d_.ny, d_.nz, cvA_, px_, "convec.xfwd", 9);
+    if (uvw_ready) {
+      SrcVort<R, true> sv{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDY], F_[LESGO_DUDZ], F_[LESGO_DVDX],
+                          F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc,
+                          kp_.plane, im};
+      xfwd<3>(sv, d_.nx, d_.ny, d_.nz, cvA_ + 3 * vol1_s_ * kp_.ninst, px_, "convec.xfwd", 6);
+    } else {
+      SrcVort<R> sv{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDY], F_[LESGO_DUDZ], F_[LESGO_DVDX],
+                    F_[LESGO_DVDZ], F_[LESGO_DWDX], F_[LESGO_DWDY], c, d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane, im};
+      xfwd<6>(sv, d_.nx, d_.ny, d_.nz, cvA_, px_, "convec.xfwd", 9);
+    }
     ypass_lin<1, 1, true, true, T2, T2>(cvA_, 0, 1, d_.nz, d_.ny, cvB_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}},
                                         "convec.ypass_pad");
     DstFields<R, 6> db{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld_big, kp_.plane_big, imb};

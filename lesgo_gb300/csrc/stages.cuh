@@ -82,8 +82,10 @@ struct SrcFields {
 };
 
 // convec.f90:71-168: u, v, w and the vorticity components (with the wall
-// and lid special cases), all scaled by 1/(nx*ny), levels 1..nz.
-template <typename R>
+// and lid special cases), all scaled by 1/(nx*ny), levels 1..nz.  With
+// VORT_ONLY the three vorticity components alone (the fused step takes the
+// velocity spectra from filt_da's forward pass).
+template <typename R, bool VORT_ONLY = false>
 struct SrcVort {
   const R *u, *v, *w, *dudy, *dudz, *dvdx, *dvdz, *dwdx, *dwdy;
   R c;
@@ -99,9 +101,11 @@ struct SrcVort {
     for (int e = 0; e < 2; ++e) {
       const long long q = o + e;
       R vals[6];
-      vals[0] = c * u[q];
-      vals[1] = c * v[q];
-      vals[2] = c * w[q];
+      if (!VORT_ONLY) {
+        vals[0] = c * u[q];
+        vals[1] = c * v[q];
+        vals[2] = c * w[q];
+      }
       R r1, r2;
       if (k == 1) {
         if (lbc == 0) {
@@ -120,9 +124,10 @@ struct SrcVort {
       vals[3] = r1;
       vals[4] = r2;
       vals[5] = c * (dvdx[q] - dudy[q]);
+      constexpr int f0 = VORT_ONLY ? 3 : 0;
 #pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        if (e == 0) out[f].x = vals[f]; else out[f].y = vals[f];
+      for (int f = f0; f < 6; ++f) {
+        if (e == 0) out[f - f0].x = vals[f]; else out[f - f0].y = vals[f];
       }
     }
   }
@@ -337,24 +342,33 @@ struct DstConvec {
     const double* c = sc + inst * SC_N;
     const R dtr = (R)c[SC_DT], t1r = (R)c[SC_T1], t2r = (R)c[SC_T2];
     const bool euler = (iflags[inst] & IF_EULER) != 0;
-    if (k <= nz - 1) {
-      R nxr = -vals[0] - divtx[q];
-      R nyr = -vals[1] - divty[q];
+    const bool in = k <= nz - 1;
+    const R zero = (R)0;
+    // every load first (the arrays may alias as far as the compiler knows,
+    // so loads after a store could not be moved ahead of it)
+    const R dx = in ? divtx[q] : zero, dy = in ? divty[q] : zero, dz = divtz[q];
+    const R ax = (turbines && in) ? fxa[q] : zero, ay = (turbines && in) ? fya[q] : zero;
+    const R az = (turbines && in) ? fza[q] : zero;
+    const R ox = in ? RHSx[q] : zero, oy = in ? RHSy[q] : zero, oz = RHSz[q];
+    const R u0 = in ? u[q] : zero, v0 = in ? v[q] : zero, w0 = w[q];
+    if (in) {
+      R nxr = -vals[0] - dx;
+      R nyr = -vals[1] - dy;
       if (use_mpf) { nxr = nxr + (R)mpfx; nyr = nyr + (R)mpfy; }
-      if (turbines) { nxr = nxr + fxa[q]; nyr = nyr + fya[q]; }
-      const R fx = euler ? nxr : RHSx[q];
-      const R fy = euler ? nyr : RHSy[q];
+      if (turbines) { nxr = nxr + ax; nyr = nyr + ay; }
+      const R fx = euler ? nxr : ox;
+      const R fy = euler ? nyr : oy;
       RHSxf[q] = fx; RHSyf[q] = fy;
       RHSx[q] = nxr; RHSy[q] = nyr;
-      u[q] = u[q] + dtr * (t1r * nxr + t2r * fx);
-      v[q] = v[q] + dtr * (t1r * nyr + t2r * fy);
+      u[q] = u0 + dtr * (t1r * nxr + t2r * fx);
+      v[q] = v0 + dtr * (t1r * nyr + t2r * fy);
     }
-    R nzr = -vals[2] - divtz[q];
-    if (turbines && k <= nz - 1) nzr = nzr + fza[q];
-    const R fz = euler ? nzr : RHSz[q];
+    R nzr = -vals[2] - dz;
+    if (turbines && in) nzr = nzr + az;
+    const R fz = euler ? nzr : oz;
     RHSzf[q] = fz;
     RHSz[q] = nzr;
-    w[q] = w[q] + dtr * (t1r * nzr + t2r * fz);
+    w[q] = w0 + dtr * (t1r * nzr + t2r * fz);
   }
 };
 
@@ -380,10 +394,11 @@ struct DstPress {
     }
     const double* c = sc + inst * SC_N;
     const R dtr = (R)c[SC_DT], t1r = (R)c[SC_T1];
-    RHSx[q] = RHSx[q] - vals[1];
-    RHSy[q] = RHSy[q] - vals[2];
-    u[q] = u[q] + dtr * (-t1r * vals[1]);
-    v[q] = v[q] + dtr * (-t1r * vals[2]);
+    const R rx = RHSx[q], ry = RHSy[q], u0 = u[q], v0 = v[q];   // loads first
+    RHSx[q] = rx - vals[1];
+    RHSy[q] = ry - vals[2];
+    u[q] = u0 + dtr * (-t1r * vals[1]);
+    v[q] = v0 + dtr * (-t1r * vals[2]);
   }
 };
 

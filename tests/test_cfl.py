@@ -80,7 +80,9 @@ def test_gpu_cfl_dropin_equals_fused(built_lib):
     b.init_ic(3)
     for _ in range(8):
         b.step_reference_order()
-    assert a.time_step() == b.time_step() and a.sim_time() == b.sim_time()
+    # the fused step reuses filt_da's x-spectra in convec: round-off apart
+    assert a.time_step() == pytest.approx(b.time_step(), rel=1e-12)
+    assert a.sim_time() == pytest.approx(b.sim_time(), rel=1e-12)
     for f in ("u", "v", "w"):
         x, y = a.get(f)[1:a.nz, :, :a.nx], b.get(f)[1:b.nz, :, :b.nx]
         assert np.max(np.abs(x - y)) <= 1e-12 * np.max(np.abs(y)), f
