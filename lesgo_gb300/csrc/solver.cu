@@ -429,6 +429,10 @@ class Solver : public SolverBase {
     err_ = alloc<int>(1);
     zo_d_ = alloc<double>(cap_);
     flags_d_ = alloc<int>(cap_);
+    // pinned staging ring for the per-step uploads (flags, averaging actions):
+    // copies from pageable memory would wait for the stream every step
+    CK(cudaMallocHost(&ring_h_, (size_t)kRing * cap_ * sizeof(int)));
+    for (auto& e : ring_ev_) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     kp_.zo_i = zo_d_;
     kp_.iflags = flags_d_;
     sc_d_ = alloc<double>((long long)SC_N * cap_);
@@ -452,6 +456,9 @@ class Solver : public SolverBase {
     for (void* p : allocs_) cudaFree(p);
     for (auto& e : ev_)
       if (e) cudaEventDestroy(e);
+    for (auto& e : ring_ev_)
+      if (e) cudaEventDestroy(e);
+    if (ring_h_) cudaFreeHost(ring_h_);
     if (st2_) cudaStreamDestroy(st2_);
     if (st_) cudaStreamDestroy(st_);
   }
@@ -789,7 +796,7 @@ class Solver : public SolverBase {
       }
     }
     if (!any) return;
-    CK(cudaMemcpyAsync(tact_d_, act.data(), act.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
+    upload_ints(tact_d_, act);
     pre();
     k_tavg_prep<<<(kp_.ninst + 63) / 64, 64, 0, st_>>>(sc_d_, tact_d_, tw_d_, kp_.ninst);
     post("tavg.prep", 0.0);
@@ -1322,6 +1329,20 @@ class Solver : public SolverBase {
     CK(cudaStreamSynchronize(st_));
   }
 
+  // Copy a small int array to the device in stream order without waiting
+  // for the stream: through the next slot of a pinned ring, reused only once
+  // the copy that last read it has run (the host runs at most kRing uploads
+  // ahead of the device).
+  void upload_ints(int* dev, const std::vector<int>& v) {
+    const int slot = (int)(ring_next_ % kRing);
+    if (ring_next_ >= kRing) CK(cudaEventSynchronize(ring_ev_[slot]));
+    int* h = ring_h_ + (size_t)slot * cap_;
+    std::memcpy(h, v.data(), v.size() * sizeof(int));
+    CK(cudaMemcpyAsync(dev, h, v.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
+    CK(cudaEventRecord(ring_ev_[slot], st_));
+    ++ring_next_;
+  }
+
   // Advance every instance's counters by one step and set its flags for the
   // step (main.f90:146-147, sgs_stag_util.f90:72-217, io.f90:557-562).
   void advance_counters() {
@@ -1359,7 +1380,7 @@ class Solver : public SolverBase {
       if (f & IF_LAG) lag = true;
       fl[s] = f;
     }
-    CK(cudaMemcpyAsync(flags_d_, fl.data(), fl.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
+    upload_ints(flags_d_, fl);
     *lag_any = lag;
     return special;
   }
@@ -1757,6 +1778,7 @@ class Solver : public SolverBase {
     };
     while (tk > 1 && smem_of(tk) > budget) tk /= 2;
     while (tk > d_.K) tk /= 2;          // tk stays a power of two
+    while (tk > 1 && d_.K % tk != 0) tk /= 2;   // no partly empty tile (K = 24 -> 8 columns)
     g.tk = tk;
     g.tk_log2 = 0;
     while ((1 << g.tk_log2) < tk) ++g.tk_log2;
@@ -2039,6 +2061,10 @@ class Solver : public SolverBase {
   T2 *cvA_ = nullptr, *cvB_ = nullptr;       // convective-term spectra
   cudaStream_t st2_ = nullptr;               // second branch of the fused step
   cudaEvent_t ev_[8] = {};
+  static constexpr int kRing = 64;
+  int* ring_h_ = nullptr;                    // pinned [kRing][cap]
+  cudaEvent_t ring_ev_[kRing] = {};
+  long long ring_next_ = 0;
   unsigned long long* cflmax_d_ = nullptr;   // per-instance |u|, |v|, |w| maxima
   int* tact_d_ = nullptr;                    // time-averaging action per instance
   double* dlog_ = nullptr;                   // diagnostics log [cap][dlog_cap_][6]
