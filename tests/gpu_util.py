@@ -48,7 +48,10 @@ def make_pair(precision: str = "fp64", seed: int = 1, **kw):
     o.set_ic(seed)
     gkw = dict(nx=p.nx, ny=p.ny, Nz=p.Nz, L_x=p.L_x, L_y=p.L_y, L_z=p.L_z, z_i=p.z_i, u_star=p.u_star,
                vonk=p.vonk, zo=p.zo, dt=p.dt, cs_count=p.cs_count, dyn_init=p.dyn_init, lbc_mom=p.lbc_mom,
-               ubc_mom=p.ubc_mom, precision=precision)
+               ubc_mom=p.ubc_mom, molec=p.molec, nu_molec=p.nu_molec, ubot=p.ubot, utop=p.utop,
+               use_mean_p_force=p.use_mean_p_force, eval_mean_p_force=p.eval_mean_p_force,
+               mean_p_force_x=p.mean_p_force_x_in, mean_p_force_y=p.mean_p_force_y_in,
+               use_cfl_dt=p.use_cfl_dt, cfl=p.cfl, precision=precision)
     g = LesgoGPU(turbines=turbines, **gkw)
     g.init_ic(seed)
     return p, o, g

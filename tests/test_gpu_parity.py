@@ -212,3 +212,32 @@ def test_pressure_solve_both_segmentations(built_lib, grid):
         e = rel_err(p, f, g.get(f), oracle_field(o, f))
         assert e < 1e-11, (grid, f, e)
     g.close()
+
+
+# Boundary conditions and physics switches of the reference beside the
+# half channel: stress-free bottom (lbc_mom 0), DNS no-slip walls with
+# molecular viscosity (1; wallstress.f90:107-170), log-law walls at both ends
+# (2), a moving DNS lid, no mean pressure gradient, and a radix-3-heavy grid.
+BC_CASES = [
+    dict(lbc_mom=0, ubc_mom=0),
+    dict(lbc_mom=1, ubc_mom=0, molec=True),
+    dict(lbc_mom=2, ubc_mom=2),
+    dict(lbc_mom=2, ubc_mom=1, molec=True, utop=0.5),
+    dict(lbc_mom=2, ubc_mom=0, molec=True),
+    dict(lbc_mom=2, ubc_mom=0, use_mean_p_force=False),
+    dict(nx=192, ny=96, Nz=12, lbc_mom=2, ubc_mom=0),
+]
+
+
+@pytest.mark.parametrize("case", BC_CASES, ids=lambda c: ",".join(f"{k}={v}" for k, v in c.items()))
+def test_boundary_conditions_and_switches(built_lib, case):
+    kw = dict(nx=32, ny=32, Nz=16, dyn_init=2, cs_count=2)
+    kw.update(case)
+    p, o, g = make_pair(**kw)
+    for _ in range(4):
+        o.step()
+    g.step(4)
+    for f in ("u", "v", "w", "p", "txz", "Cs_opt2"):
+        e = rel_err(p, f, g.get(f), oracle_field(o, f))
+        assert e < 1e-10, (case, f, e)
+    g.close()
