@@ -340,49 +340,118 @@ struct YGeom {
   long long out_lev_stride;
   int tk_log2;               // tk is a power of two
   FastDiv fny_in, fny_out;
+  FastDiv fwin;              // by NIN * tk (the width of the input tile)
+  FastDiv ftk;               // by tk (the width of an output tile)
 };
+
+// Stockham FFT along y of the columns of a row-major tile: element y of
+// column l at a[y * width + l].  Threads run over (butterfly, column) with
+// the column fastest, so a warp touches consecutive addresses at every step
+// (no bank conflicts); the butterflies are those of fft_lines.
+template <typename R, bool INV>
+__device__ cplx<R>* fft_cols(cplx<R>* a, cplx<R>* b, int width, const FastDiv& fw, const FftPlan<R>& p) {
+  using T2 = cplx<R>;
+  for (int s = 0; s < p.nf; ++s) {
+    const int Rr = p.radix[s];
+    const int nb = p.nbs[s];
+    const int Ns = p.nss[s];
+    const int total = nb * width;
+    const int tws = nb / Ns;
+    const FastDiv fns = p.fns[s];
+    const int sr = nb * width, sd = Ns * width;   // strides between a butterfly's inputs / outputs
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int j = fw.div(t);
+      const int l = t - j * width;
+      const int q = fns.div(j);
+      const int jm = j - q * Ns;
+      const T2* src = a + j * width + l;
+      T2* dst = b + (q * Ns * Rr + jm) * width + l;
+      const int tb = jm * tws;
+      if (Rr == 4) {
+        T2 v0 = src[0], v1 = src[sr], v2 = src[2 * sr], v3 = src[3 * sr];
+        if (tb) {
+          v1 = twid<T2, INV>(p.tw, tb, v1);
+          v2 = twid<T2, INV>(p.tw, 2 * tb, v2);
+          v3 = twid<T2, INV>(p.tw, 3 * tb, v3);
+        }
+        bfly4<T2, INV>(v0, v1, v2, v3);
+        dst[0] = v0; dst[sd] = v1; dst[2 * sd] = v2; dst[3 * sd] = v3;
+      } else if (Rr == 8) {
+        T2 v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = src[r * sr];
+        if (tb) {
+#pragma unroll
+          for (int r = 1; r < 8; ++r) v[r] = twid<T2, INV>(p.tw, r * tb, v[r]);
+        }
+        bfly8<T2, INV>(v);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) dst[r * sd] = v[r];
+      } else if (Rr == 2) {
+        T2 v0 = src[0], v1 = src[sr];
+        if (tb) v1 = twid<T2, INV>(p.tw, tb, v1);
+        bfly2<T2, INV>(v0, v1);
+        dst[0] = v0; dst[sd] = v1;
+      } else {  // 3
+        T2 v0 = src[0], v1 = src[sr], v2 = src[2 * sr];
+        if (tb) {
+          v1 = twid<T2, INV>(p.tw, tb, v1);
+          v2 = twid<T2, INV>(p.tw, 2 * tb, v2);
+        }
+        bfly3<T2, INV>(v0, v1, v2);
+        dst[0] = v0; dst[sd] = v1; dst[2 * sd] = v2;
+      }
+    }
+    __syncthreads();
+    cplx<R>* tmp = a; a = b; b = tmp;
+  }
+  return a;
+}
 
 // Y pass.  NIN input spectra (after Xf) are loaded per column tile and, if
 // FWD, transformed along y.  Each of NOUT outputs is a combination
 // sum_i coef(o, i, kx, ky) * F_i(ky), mapped to ny_out rows (3/2 padding or
 // truncation), inverse transformed if INV, and stored.  Op supplies
-// pointers, coefficients and the row map.
+// pointers, coefficients and the row map.  Tiles are row-major: input i,
+// row y, column c at S[y * NIN * tk + i * tk + c]; outputs W[y * tk + c].
 template <typename R, int NIN, int NOUT, bool FWD, bool INV, class Op>
 __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<R> pout, Op op) {
   using T2 = cplx<R>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // S: NIN*tk input lines (ls_in).  X: scratch of max(NIN*tk*ls_in, 2*tk*ls_out)
-  // elements; W0/W1 (tk lines of ls_out each) alias its front.
+  // S: the NIN*tk input columns (ny_in rows).  X: scratch of
+  // max(NIN*tk*ny_in, 2*tk*ny_out) elements; W0/W1 (tk columns of ny_out
+  // rows each) alias its front.
+  const int win = NIN * g.tk;
   T2* S = reinterpret_cast<T2*>(smem_raw);
-  T2* X = S + NIN * g.tk * g.ls_in;
+  T2* X = S + win * g.ny_in;
   T2* W0 = X;
-  T2* W1 = X + g.tk * g.ls_out;
+  T2* W1 = X + g.tk * g.ny_out;
   const int kx0 = blockIdx.x * g.tk;
   const int li = blockIdx.y;
   const int grp = blockIdx.z;
   const int tk = min(g.tk, g.K - kx0);
-  // load inputs: element (jy, c) of input i
-  #pragma unroll 4
-  for (int t = threadIdx.x; t < NIN * g.ny_in * g.tk; t += blockDim.x) {
-    const int c = t & (g.tk - 1);
-    const int rest = t >> g.tk_log2;
-    const int i = g.fny_in.div(rest);
-    const int jy = rest - i * g.ny_in;
+  // load inputs: column c of input i at row jy
+#pragma unroll 4
+  for (int t = threadIdx.x; t < win * g.ny_in; t += blockDim.x) {
+    const int jy = g.fwin.div(t);
+    const int col = t - jy * win;
+    const int i = col >> g.tk_log2;
+    const int c = col & (g.tk - 1);
     T2 v = mkc((R)0, (R)0);
     if (c < tk) v = op.load(grp, i, li, jy, kx0 + c);
-    S[(i * g.tk + c) * g.ls_in + jy] = v;
+    S[t] = v;
   }
   __syncthreads();
   if (FWD) {
-    T2* res = fft_lines<R, false>(S, X, NIN * g.tk, g.ls_in, pin);
+    T2* res = fft_cols<R, false>(S, X, win, g.fwin, pin);
     if (res != S) {
-      for (int t = threadIdx.x; t < NIN * g.tk * g.ls_in; t += blockDim.x) S[t] = res[t];
+      for (int t = threadIdx.x; t < win * g.ny_in; t += blockDim.x) S[t] = res[t];
       __syncthreads();
     }
   }
   for (int o = 0; o < NOUT; ++o) {
     for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
-      const int c = g.fny_out.div(t), ky = t - c * g.ny_out;
+      const int ky = t >> g.tk_log2, c = t & (g.tk - 1);
       const int kx = kx0 + c;
       T2 acc = mkc((R)0, (R)0);
       const int kin = op.rowmap(ky);
@@ -391,20 +460,20 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
         for (int i = 0; i < NIN; ++i) {
           T2 cf;
           if (op.coef(grp, o, i, kx, kin, cf)) {
-            T2 s = S[(i * g.tk + c) * g.ls_in + kin];
+            T2 s = S[kin * win + i * g.tk + c];
             acc = cadd(acc, cmul(s, cf));
           }
         }
       }
-      W0[c * g.ls_out + ky] = acc;
+      W0[t] = acc;
     }
     __syncthreads();
     T2* res = W0;
-    if (INV) res = fft_lines<R, true>(W0, W1, g.tk, g.ls_out, pout);
-    #pragma unroll 4
+    if (INV) res = fft_cols<R, true>(W0, W1, g.tk, g.ftk, pout);
+#pragma unroll 4
     for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
       const int ky = t >> g.tk_log2, c = t & (g.tk - 1);
-      if (c < tk) op.store(grp, o, li, ky, kx0 + c, res[c * g.ls_out + ky]);
+      if (c < tk) op.store(grp, o, li, ky, kx0 + c, res[t]);
     }
     __syncthreads();
   }

@@ -1773,8 +1773,8 @@ class Solver : public SolverBase {
     const size_t budget = ybudget_;
     int tk = sizeof(R) == 8 ? 8 : 16;
     auto smem_of = [&](int t) {
-      const size_t s = (size_t)NIN * t * g.ls_in;
-      return (s + std::max(s, (size_t)2 * t * g.ls_out)) * sizeof(T2);
+      const size_t s = (size_t)NIN * t * g.ny_in;
+      return (s + std::max(s, (size_t)2 * t * g.ny_out)) * sizeof(T2);
     };
     while (tk > 1 && smem_of(tk) > budget) tk /= 2;
     while (tk > d_.K) tk /= 2;          // tk stays a power of two
@@ -1783,6 +1783,8 @@ class Solver : public SolverBase {
     g.tk_log2 = 0;
     while ((1 << g.tk_log2) < tk) ++g.tk_log2;
     g.fny_in = FastDiv((unsigned)in_rows); g.fny_out = FastDiv((unsigned)out_rows);
+    g.fwin = FastDiv((unsigned)(NIN * tk));
+    g.ftk = FastDiv((unsigned)tk);
     g.in_lev_stride = 0; g.out_lev_stride = 0;
     const size_t smem = smem_of(tk);
     auto kern = k_ypass<R, NIN, NOUT, FWD, INV, YOpLin<R, NIN, NOUT, InT, OutT>>;
