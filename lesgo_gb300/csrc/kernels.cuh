@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_column(ColArgs<R> a) {
   const long long c0 = inst * kp.istride + (long long)j * kp.ld + i;  // 3-D fields
   const double zo = kp.zo_i[inst];
   const bool cs_fill = (kp.iflags[inst] & IF_CSFILL) != 0;
-  const R inv_dz = (R)(1.0 / kp.dz);
+  const R inv_dz = (R)kp.idz;
   const R h = (R)0.5;
 
   // wall values (needed at k = 1 and k = nz)
@@ -235,15 +235,19 @@ __global__ void __launch_bounds__(256) k_column(ColArgs<R> a) {
 }
 
 // Flat thread index over (instance, level 1..nz, j, i < nx) -> field offset.
+// Point index t (x fastest, then y, level 1..nz, instance) -> coordinates.
+// Launches cover fewer than 2^31 points (checked when a handle is made), so
+// the decomposition divides 32-bit values by multiply-high reciprocals.
 struct PtIdx { int inst, k, j, i; long long q; };
 __device__ __forceinline__ PtIdx pt_index(long long t, const KP& kp) {
   PtIdx r;
-  r.i = (int)(t % kp.nx);
-  long long rr = t / kp.nx;
-  r.j = (int)(rr % kp.ny);
-  rr /= kp.ny;
-  r.k = 1 + (int)(rr % kp.nz);
-  r.inst = (int)(rr / kp.nz);
+  const int ti = (int)t;
+  const int a = kp.fnx.div(ti);
+  r.i = ti - a * kp.nx;
+  const int b = kp.fny.div(a);
+  r.j = a - b * kp.ny;
+  r.inst = kp.fnz.div(b);
+  r.k = 1 + (b - r.inst * kp.nz);
   r.q = r.inst * kp.istride + (long long)r.k * kp.plane + (long long)r.j * kp.ld + r.i;
   return r;
 }
@@ -257,7 +261,7 @@ __global__ void k_ddz(const R* __restrict__ f, R* __restrict__ dfdz, KP kp) {
     const PtIdx x = pt_index(t, kp);
     const int k = x.k;
     const long long q = x.q;
-    const R c = (R)(1.0 / kp.dz);
+    const R c = (R)kp.idz;
     if (UV) { if (k >= 2) dfdz[q] = c * (f[q] - f[q - kp.plane]); }
     else    { if (k <= kp.nz - 1) dfdz[q] = c * (f[q + kp.plane] - f[q]); }
   }
@@ -333,10 +337,10 @@ __global__ void k_interp(InterpArgs<R> a) {
   // divisions by at most an ulp, and a cell flip at an exact face leaves the
   // linear interpolant unchanged
   const double thresh = 1.0e-9;
-  const double idx = 1.0 / kp.dx, idy = 1.0 / kp.dy, idz = 1.0 / dz;
-  double px = xq - floor(xq * (1.0 / kp.L_x)) * kp.L_x;
+  const double idx = kp.idx, idy = kp.idy, idz = kp.idz;   // reciprocals made on the host
+  double px = xq - floor(xq * kp.iLx) * kp.L_x;
   int ist = (fabs(px) < thresh * kp.L_x) ? 1 : (fabs(px - kp.L_x) < thresh * kp.L_x) ? kp.nx : (int)floor(px * idx) + 1;
-  double py = yq - floor(yq * (1.0 / kp.L_y)) * kp.L_y;
+  double py = yq - floor(yq * kp.iLy) * kp.L_y;
   int jst = (fabs(py) < thresh * kp.L_y) ? 1 : (fabs(py - kp.L_y) < thresh * kp.L_y) ? kp.ny : (int)floor(py * idy) + 1;
   ist = min(max(ist, 1), kp.nx);
   jst = min(max(jst, 1), kp.ny);
@@ -405,7 +409,7 @@ struct ThomasArgs {
   double2* phat;                 // levels 0..nz, [inst][nz+1][P]; holds r, then u
   const double *ibet, *gam;      // [n+1][P], index j = 1..n (shared by instances)
   const double *kxw, *kyw;
-  double dz;
+  double dz, idz, idz2;   // dz, 1/dz, 1/dz^2 (made on the host)
   int nz, ny, K, ninst;
 };
 
@@ -415,7 +419,7 @@ __device__ __forceinline__ double2 thomas_rhs(const ThomasArgs& a, const double2
   const int nz = a.nz;
   if (j == 1) { const double2 h = Hb[t]; return make_double2(-a.dz * h.x, -a.dz * h.y); }
   if (j == nz + 1) { const double2 h = Ht[t]; return make_double2(-a.dz * h.x, -a.dz * h.y); }
-  const double c4 = 1.0 / a.dz;
+  const double c4 = a.idz;
   const double2 hx = Hx[(j - 2) * P + t], hy = Hy[(j - 2) * P + t];
   const double2 hz = Hz[(j - 1) * P + t], hzp = Hz[(j - 2) * P + t];
   // i kx Hx(j-1) + i ky Hy(j-1) + (Hz(j) - Hz(j-1)) / dz
@@ -445,7 +449,7 @@ __global__ void __launch_bounds__(SEG * COLS) k_thomas(ThomasArgs a) {
   const bool mean = kx == 0 && jy == 0;
   const int L = (n + SEG - 1) / SEG;
   const int j0 = 1 + seg * L, j1 = min(n, j0 + L - 1);   // this thread's levels (may be empty)
-  const double c3 = 1.0 / (a.dz * a.dz);
+  const double c3 = a.idz2;
   const double kxv = a.kxw[kx], kyv = a.kyw[jy];
   const bool solve = live && !nyq && !mean;
 
@@ -544,7 +548,9 @@ __global__ void k_wproj(const R* __restrict__ p, R* dpdz, R* RHSz, R* u, R* v, R
   const int k = x.k;
   const long long P = kp.plane;
   const long long q = x.q;
-  const R d = (p[q] - p[q - P]) / (R)kp.dz;
+  // (p(k) - p(k-1)) / dz as a multiply by 1/dz: within an ulp of the
+  // division, which is a long instruction sequence in FP64 on this part
+  const R d = (p[q] - p[q - P]) * (R)kp.idz;
   if (!FUSED) { dpdz[q] = d; return; }
   RHSz[q] = RHSz[q] - d;
   const int nz = kp.nz;
@@ -1010,10 +1016,11 @@ __global__ void __launch_bounds__(256) k_cfl_max(const R* u, const R* v, const R
   const long long base = inst * kp.istride + kp.plane;
   double au = 0.0, av = 0.0, aw = 0.0;
   for (long long t = blockIdx.x * 256LL + threadIdx.x; t < m; t += (long long)gridDim.x * 256) {
-    const int i = (int)(t % kp.nx);
-    const long long r = t / kp.nx;
-    const int j = (int)(r % kp.ny);
-    const long long k = r / kp.ny;   // 0 .. nz-2 (level k + 1)
+    const int ti = (int)t;
+    const int r = kp.fnx.div(ti);
+    const int i = ti - r * kp.nx;
+    const int k = kp.fny.div(r);     // 0 .. nz-2 (level k + 1)
+    const int j = r - k * kp.ny;
     const long long q = base + k * kp.plane + (long long)j * kp.ld + i;
     au = fmax(au, fabs((double)u[q]));
     av = fmax(av, fabs((double)v[q]));

@@ -404,6 +404,11 @@ class Solver : public SolverBase {
     kp_.turbines = 0;
     kp_.ninst = 0;
     kp_.istride = (long long)(nz + 1) * kp_.plane;
+    kp_.fnx = FastDiv((unsigned)nx); kp_.fny = FastDiv((unsigned)ny); kp_.fnz = FastDiv((unsigned)nz);
+    kp_.idx = 1.0 / kp_.dx; kp_.idy = 1.0 / kp_.dy; kp_.idz = 1.0 / kp_.dz;
+    kp_.iLx = 1.0 / kp_.L_x; kp_.iLy = 1.0 / kp_.L_y;
+    if ((long long)nx * ny * (nz + 1) * capacity >= (1LL << 31))
+      throw Error(LESGO_ERR_UNSUPPORTED, "more than 2^31 grid points in one handle");
     kp_.istride_big = (long long)(nz + 1) * kp_.plane_big;
     nfield_ = kp_.istride * cap_;
     for (int f = 0; f < LESGO_NFIELDS; ++f) F_[f] = alloc<R>(nfield_);
@@ -1986,7 +1991,8 @@ class Solver : public SolverBase {
     ta.Hb = hplane_; ta.Ht = hplane_ + pl_s;
     ta.phat = phat_; ta.ibet = ibet_; ta.gam = tgam_;
     ta.kxw = kxw64_; ta.kyw = kyw64_;
-    ta.dz = d_.dz; ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.ninst = kp_.ninst;
+    ta.dz = d_.dz; ta.idz = 1.0 / d_.dz; ta.idz2 = 1.0 / (d_.dz * d_.dz);
+    ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.ninst = kp_.ninst;
     pre();
     // 16 segments per column when 8 would leave most SMs idle
     const long long ncol = pl_s * kp_.ninst;

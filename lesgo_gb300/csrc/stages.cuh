@@ -20,6 +20,8 @@ struct KP {
   const double* zo_i;        // per-instance roughness length
   const int* iflags;         // per-instance step flags (IF_*)
   const double* sc;          // per-instance step constants [inst][SC_N] (SC_*)
+  FastDiv fnx, fny, fnz;     // by nx, ny, nz (point-index decomposition)
+  double idx, idy, idz, iLx, iLy;   // 1/dx, 1/dy, 1/dz, 1/L_x, 1/L_y
 };
 
 // Per-instance step constants, resident on the device so that a time step
