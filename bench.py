@@ -308,7 +308,10 @@ def time_batched(args, torch):
 def time_e2e_batched(args, torch):
     """The batched ensemble through the C ABI with host buffers: per step,
     every instance's u, v, w go host->device from pinned FP64 memory, all
-    classes step once, and u, v, w of every instance come back."""
+    classes step once, and u, v, w of every instance come back.  The copies
+    are queued in stream order (the *_async calls): each class's copies run
+    on its handle's stream while the other classes' steps run, and a step's
+    uploads read the buffers its predecessor's downloads wrote."""
     batches = make_batches("mixed")
     step_all(batches, 10)
     host = []
@@ -323,15 +326,20 @@ def time_e2e_batched(args, torch):
             host.append((b, iid, bufs))
     steps = max(5, (args.steps + 4) // 5 * 5)
 
+    by_batch = {}
+    for b, iid, bufs in host:
+        by_batch.setdefault(id(b), (b, []))[1].append((iid, bufs))
+
     def run():
         for _ in range(steps):
-            for b, iid, bufs in host:
-                for k, t in bufs.items():
-                    b.set_ptr(iid, k, t.data_ptr(), 0, b.nz)
-            step_all(batches, 1)
-            for b, iid, bufs in host:
-                for k, t in bufs.items():
-                    b.get_ptr(iid, k, t.data_ptr(), 0, b.nz)
+            for b, lst in by_batch.values():
+                for iid, bufs in lst:
+                    for k, t in bufs.items():
+                        b.set_ptr(iid, k, t.data_ptr(), 0, b.nz, wait=False)
+                b.step(1)
+                for iid, bufs in lst:
+                    for k, t in bufs.items():
+                        b.get_ptr(iid, k, t.data_ptr(), 0, b.nz, wait=False)
 
     ms = timed_on_device(torch, batches, run)
     pts = sum(g[0] * g[1] * g[2] * len(ids) for g, ids, _ in batches)

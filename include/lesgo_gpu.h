@@ -134,6 +134,13 @@ int lesgo_gpu_dims(const lesgo_handle_t* h, int* nz, int* ld, int* lh, int* nx2,
  * / out of the device field (levels outside 0..nz are rejected). */
 int lesgo_gpu_set_field(lesgo_handle_t* h, int field, const double* host, int lbz, int nzhi);
 int lesgo_gpu_get_field(lesgo_handle_t* h, int field, double* host, int lbz, int nzhi);
+/* The same copies in stream order: they return once queued, behind the
+ * handle's queued steps.  The host array must stay unchanged (set) and
+ * unread (get) until lesgo_gpu_sync or a synchronous call on the handle;
+ * with page-locked host memory the copies run while the host continues (and
+ * while other handles' steps run on the device). */
+int lesgo_gpu_set_field_async(lesgo_handle_t* h, int field, const double* host, int lbz, int nzhi);
+int lesgo_gpu_get_field_async(lesgo_handle_t* h, int field, double* host, int lbz, int nzhi);
 
 /* Field registry: remember a Fortran module array (c_loc) for a field, then
  * upload/download it on demand (init, checkpoint and output only). */
@@ -245,6 +252,8 @@ int lesgo_gpu_batch_remove(lesgo_handle_t* h, int id);
 int lesgo_gpu_batch_size(const lesgo_handle_t* h, int* active, int* capacity);
 int lesgo_gpu_set_field_inst(lesgo_handle_t* h, int id, int field, const double* host, int lbz, int nzhi);
 int lesgo_gpu_get_field_inst(lesgo_handle_t* h, int id, int field, double* host, int lbz, int nzhi);
+int lesgo_gpu_set_field_inst_async(lesgo_handle_t* h, int id, int field, const double* host, int lbz, int nzhi);
+int lesgo_gpu_get_field_inst_async(lesgo_handle_t* h, int id, int field, double* host, int lbz, int nzhi);
 int lesgo_gpu_diag_inst(lesgo_handle_t* h, int id, double* rmsdiv, double* ke, double* cfl, double* tau_bot);
 int lesgo_gpu_counters_inst(lesgo_handle_t* h, int id, int* jt, int* jt_total);
 int lesgo_gpu_turbine_state_inst(lesgo_handle_t* h, int id, double* u_d_T, double* f_n, double* power, int n);

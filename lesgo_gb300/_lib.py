@@ -73,6 +73,8 @@ SIGNATURES = {
     "lesgo_gpu_dims": (_I, [_H, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_set_field": (_I, [_H, _I, C.c_void_p, _I, _I]),
     "lesgo_gpu_get_field": (_I, [_H, _I, C.c_void_p, _I, _I]),
+    "lesgo_gpu_set_field_async": (_I, [_H, _I, C.c_void_p, _I, _I]),
+    "lesgo_gpu_get_field_async": (_I, [_H, _I, C.c_void_p, _I, _I]),
     "lesgo_gpu_bind_field": (_I, [_H, _I, C.c_void_p, _I, _I]),
     "lesgo_gpu_upload": (_I, [_H, _I]),
     "lesgo_gpu_download": (_I, [_H, _I]),
@@ -111,6 +113,8 @@ SIGNATURES = {
     "lesgo_gpu_batch_size": (_I, [_H, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_set_field_inst": (_I, [_H, _I, _I, C.c_void_p, _I, _I]),
     "lesgo_gpu_get_field_inst": (_I, [_H, _I, _I, C.c_void_p, _I, _I]),
+    "lesgo_gpu_set_field_inst_async": (_I, [_H, _I, _I, C.c_void_p, _I, _I]),
+    "lesgo_gpu_get_field_inst_async": (_I, [_H, _I, _I, C.c_void_p, _I, _I]),
     "lesgo_gpu_diag_inst": (_I, [_H, _I, _D, _D, _D, _D]),
     "lesgo_gpu_counters_inst": (_I, [_H, _I, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_turbine_state_inst": (_I, [_H, _I, _D, _D, _D, _I]),

@@ -322,8 +322,9 @@ class SolverBase {
   virtual int active() const = 0;
   virtual int add_instance(const InstanceSpec& spec) = 0;
   virtual void remove_instance(int id) = 0;
-  virtual void set_field(int id, int f, const double* h, int lbz, int nzhi) = 0;
-  virtual void get_field(int id, int f, double* h, int lbz, int nzhi) = 0;
+  // wait = false: stream-ordered, returns once the copy is queued
+  virtual void set_field(int id, int f, const double* h, int lbz, int nzhi, bool wait = true) = 0;
+  virtual void get_field(int id, int f, double* h, int lbz, int nzhi, bool wait = true) = 0;
   virtual void init_ic(int id, uint64_t seed) = 0;
   virtual void filt_da(int f, int dx, int dy) = 0;
   virtual void ddxy(int f, int dx, int dy) = 0;   // dx or dy may be -1
@@ -524,7 +525,7 @@ class Solver : public SolverBase {
     if (f < 0 || f >= LESGO_NFIELDS) throw Error(LESGO_ERR_ARG, "bad field id");
     if (lbz < 0 || nzhi > d_.nz || nzhi < lbz) throw Error(LESGO_ERR_ARG, "levels outside 0..nz");
   }
-  void set_field(int id, int f, const double* h, int lbz, int nzhi) override {
+  void set_field(int id, int f, const double* h, int lbz, int nzhi, bool wait = true) override {
     check_range(f, lbz, nzhi);
     const int slot = slot_of(id);
     const long long n = (long long)(nzhi - lbz + 1) * kp_.plane;
@@ -537,9 +538,9 @@ class Solver : public SolverBase {
       k_convert<double, R><<<grid1(n), 256, 0, st_>>>(stg, dst, n);
       post();
     }
-    CK(cudaStreamSynchronize(st_));
+    if (wait) CK(cudaStreamSynchronize(st_));
   }
-  void get_field(int id, int f, double* h, int lbz, int nzhi) override {
+  void get_field(int id, int f, double* h, int lbz, int nzhi, bool wait = true) override {
     check_range(f, lbz, nzhi);
     const int slot = slot_of(id);
     const long long n = (long long)(nzhi - lbz + 1) * kp_.plane;
@@ -552,7 +553,7 @@ class Solver : public SolverBase {
       post();
       CK(cudaMemcpyAsync(h, stg, n * sizeof(double), cudaMemcpyDeviceToHost, st_));
     }
-    CK(cudaStreamSynchronize(st_));
+    if (wait) CK(cudaStreamSynchronize(st_));
   }
 
   void init_ic(int id, uint64_t seed) override {
@@ -2215,6 +2216,14 @@ int lesgo_gpu_get_field(lesgo_handle_t* h, int f, double* host, int lbz, int nzh
   if (!host) return LESGO_ERR_ARG;
   return guarded(h, [&] { h->s->get_field(h->inst0, f, host, lbz, nzhi); });
 }
+int lesgo_gpu_set_field_async(lesgo_handle_t* h, int f, const double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->set_field(h->inst0, f, host, lbz, nzhi, false); });
+}
+int lesgo_gpu_get_field_async(lesgo_handle_t* h, int f, double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->get_field(h->inst0, f, host, lbz, nzhi, false); });
+}
 int lesgo_gpu_bind_field(lesgo_handle_t* h, int f, double* host, int lbz, int nzhi) {
   if (!h || !h->s || !host || f < 0 || f >= LESGO_NFIELDS) return LESGO_ERR_ARG;
   if (lbz < 0 || nzhi > h->s->der().nz || nzhi < lbz) return LESGO_ERR_ARG;
@@ -2478,6 +2487,14 @@ int lesgo_gpu_set_field_inst(lesgo_handle_t* h, int id, int f, const double* hos
 int lesgo_gpu_get_field_inst(lesgo_handle_t* h, int id, int f, double* host, int lbz, int nzhi) {
   if (!host) return LESGO_ERR_ARG;
   return guarded(h, [&] { h->s->get_field(id, f, host, lbz, nzhi); });
+}
+int lesgo_gpu_set_field_inst_async(lesgo_handle_t* h, int id, int f, const double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->set_field(id, f, host, lbz, nzhi, false); });
+}
+int lesgo_gpu_get_field_inst_async(lesgo_handle_t* h, int id, int f, double* host, int lbz, int nzhi) {
+  if (!host) return LESGO_ERR_ARG;
+  return guarded(h, [&] { h->s->get_field(id, f, host, lbz, nzhi, false); });
 }
 int lesgo_gpu_diag_inst(lesgo_handle_t* h, int id, double* rmsdiv, double* ke, double* cfl, double* tau_bot) {
   double out[4] = {0, 0, 0, 0};

@@ -171,12 +171,17 @@ class LesgoGPU:
             raise ValueError(f"expected (levels, {self.ny}, {self.ld}), got {a.shape}")
         self._check(self._lib.lesgo_gpu_set_field(self._h, self._fid(name), a.ctypes.data, lbz, lbz + a.shape[0] - 1))
 
-    def set_ptr(self, name, ptr: int, lbz: int, nzhi: int):
-        """Copy levels lbz..nzhi from a host FP64 buffer at address ``ptr``."""
-        self._check(self._lib.lesgo_gpu_set_field(self._h, self._fid(name), C.c_void_p(ptr), lbz, nzhi))
+    def set_ptr(self, name, ptr: int, lbz: int, nzhi: int, wait: bool = True):
+        """Copy levels lbz..nzhi from a host FP64 buffer at address ``ptr``.
+        wait=False queues the copy in stream order (the buffer must stay
+        unchanged until sync())."""
+        fn = self._lib.lesgo_gpu_set_field if wait else self._lib.lesgo_gpu_set_field_async
+        self._check(fn(self._h, self._fid(name), C.c_void_p(ptr), lbz, nzhi))
 
-    def get_ptr(self, name, ptr: int, lbz: int, nzhi: int):
-        self._check(self._lib.lesgo_gpu_get_field(self._h, self._fid(name), C.c_void_p(ptr), lbz, nzhi))
+    def get_ptr(self, name, ptr: int, lbz: int, nzhi: int, wait: bool = True):
+        """wait=False queues the copy; the buffer holds the data after sync()."""
+        fn = self._lib.lesgo_gpu_get_field if wait else self._lib.lesgo_gpu_get_field_async
+        self._check(fn(self._h, self._fid(name), C.c_void_p(ptr), lbz, nzhi))
 
     def init_ic(self, seed: int):
         self._check(self._lib.lesgo_gpu_init_ic(self._h, C.c_uint64(seed)))
@@ -438,12 +443,15 @@ class LesgoBatch:
         self._check(self._lib.lesgo_gpu_get_field_inst(self._h, iid, LesgoGPU._fid(name), out.ctypes.data, lbz, nzhi))
         return out
 
-    def set_ptr(self, iid: int, name, ptr: int, lbz: int, nzhi: int):
-        """Copy levels lbz..nzhi of instance iid from a host FP64 buffer at ``ptr``."""
-        self._check(self._lib.lesgo_gpu_set_field_inst(self._h, iid, LesgoGPU._fid(name), C.c_void_p(ptr), lbz, nzhi))
+    def set_ptr(self, iid: int, name, ptr: int, lbz: int, nzhi: int, wait: bool = True):
+        """Copy levels lbz..nzhi of instance iid from a host FP64 buffer at
+        ``ptr``; wait=False queues it in stream order (see LesgoGPU.set_ptr)."""
+        fn = self._lib.lesgo_gpu_set_field_inst if wait else self._lib.lesgo_gpu_set_field_inst_async
+        self._check(fn(self._h, iid, LesgoGPU._fid(name), C.c_void_p(ptr), lbz, nzhi))
 
-    def get_ptr(self, iid: int, name, ptr: int, lbz: int, nzhi: int):
-        self._check(self._lib.lesgo_gpu_get_field_inst(self._h, iid, LesgoGPU._fid(name), C.c_void_p(ptr), lbz, nzhi))
+    def get_ptr(self, iid: int, name, ptr: int, lbz: int, nzhi: int, wait: bool = True):
+        fn = self._lib.lesgo_gpu_get_field_inst if wait else self._lib.lesgo_gpu_get_field_inst_async
+        self._check(fn(self._h, iid, LesgoGPU._fid(name), C.c_void_p(ptr), lbz, nzhi))
 
     def set(self, iid: int, name, arr: np.ndarray, lbz: int = 0):
         a = np.ascontiguousarray(arr, dtype=np.float64)
