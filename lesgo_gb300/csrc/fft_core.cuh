@@ -147,62 +147,71 @@ __device__ __forceinline__ T2 twid(const T2* tw, int idx, T2 a) {
   return INV ? cmulconj(a, w) : cmul(a, w);
 }
 
+// Radix-RR butterfly on registers.
+template <typename T2, bool INV, int RR>
+__device__ __forceinline__ void bfly(T2* v) {
+  if constexpr (RR == 8) bfly8<T2, INV>(v);
+  else if constexpr (RR == 4) bfly4<T2, INV>(v[0], v[1], v[2], v[3]);
+  else if constexpr (RR == 3) bfly3<T2, INV>(v[0], v[1], v[2]);
+  else bfly2<T2, INV>(v[0], v[1]);
+}
+
+// One Stockham stage of radix RR over `total` butterflies.  Butterfly t is
+// (line or column, j); `at(t, j)` gives the offset of its first input and
+// `out(t, j)` the offset of output 0 of a butterfly with q = j / Ns, jm = j
+// % Ns: inputs at src + r * sr, outputs at dst + r * sd (r < RR).  FIRST
+// marks the first stage (Ns = 1: no twiddles, q = j).  The twiddles of
+// butterfly jm are tw[r * jm * tws]; jm = 0 multiplies by tw[0] = 1 exactly,
+// which keeps the warp on one path.
+template <typename T2, bool INV, int RR, bool FIRST>
+__device__ __forceinline__ void stage_bfly(const T2* src, T2* dst, int sr, int sd, const T2* tw, int tb) {
+  T2 v[RR];
+#pragma unroll
+  for (int r = 0; r < RR; ++r) v[r] = src[r * sr];
+  if (!FIRST) {
+#pragma unroll
+    for (int r = 1; r < RR; ++r) v[r] = twid<T2, INV>(tw, r * tb, v[r]);
+  }
+  bfly<T2, INV, RR>(v);
+#pragma unroll
+  for (int r = 0; r < RR; ++r) dst[r * sd] = v[r];
+}
+
+template <typename T2, bool INV, int RR, bool FIRST>
+__device__ __forceinline__ void lines_stage(const T2* a, T2* b, int nl, int ls, int nb, int Ns, int tws,
+                                            const FastDiv& fnb, const FastDiv& fns, const T2* tw) {
+  const int total = nl * nb;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int l = fnb.div(t);
+    const int j = t - l * nb;
+    const int q = FIRST ? j : fns.div(j);
+    const int jm = j - q * Ns;
+    stage_bfly<T2, INV, RR, FIRST>(a + l * ls + j, b + l * ls + q * Ns * RR + jm, nb, Ns, tw, jm * tws);
+  }
+}
+
+template <typename T2, bool INV, bool FIRST>
+__device__ __forceinline__ void lines_stage_r(int Rr, const T2* a, T2* b, int nl, int ls, int nb, int Ns, int tws,
+                                              const FastDiv& fnb, const FastDiv& fns, const T2* tw) {
+  switch (Rr) {
+    case 8: lines_stage<T2, INV, 8, FIRST>(a, b, nl, ls, nb, Ns, tws, fnb, fns, tw); break;
+    case 4: lines_stage<T2, INV, 4, FIRST>(a, b, nl, ls, nb, Ns, tws, fnb, fns, tw); break;
+    case 3: lines_stage<T2, INV, 3, FIRST>(a, b, nl, ls, nb, Ns, tws, fnb, fns, tw); break;
+    default: lines_stage<T2, INV, 2, FIRST>(a, b, nl, ls, nb, Ns, tws, fnb, fns, tw); break;
+  }
+}
+
 // Stockham autosort FFT of `nl` lines of length p.n held in shared memory
 // (line l at a + l*ls).  `b` is scratch of the same shape.  Returns the
 // buffer that holds the result.  All threads of the block must call it.
 template <typename R, bool INV>
 __device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FftPlan<R>& p) {
-  using T2 = cplx<R>;
   for (int s = 0; s < p.nf; ++s) {
-    const int Rr = p.radix[s];
-    const int nb = p.nbs[s];
-    const int Ns = p.nss[s];
-    const int total = nl * nb;
-    const int tws = nb / Ns;            // n / (Ns * Rr)
-    const FastDiv fnb = p.fnb[s], fns = p.fns[s];
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int l = fnb.div(t);
-      const int j = t - l * nb;
-      const int q = fns.div(j);
-      const int jm = j - q * Ns;
-      const T2* src = a + l * ls + j;
-      T2* dst = b + l * ls + q * Ns * Rr + jm;
-      const int tb = jm * tws;
-      if (Rr == 4) {
-        T2 v0 = src[0], v1 = src[nb], v2 = src[2 * nb], v3 = src[3 * nb];
-        if (tb) {
-          v1 = twid<T2, INV>(p.tw, tb, v1);
-          v2 = twid<T2, INV>(p.tw, 2 * tb, v2);
-          v3 = twid<T2, INV>(p.tw, 3 * tb, v3);
-        }
-        bfly4<T2, INV>(v0, v1, v2, v3);
-        dst[0] = v0; dst[Ns] = v1; dst[2 * Ns] = v2; dst[3 * Ns] = v3;
-      } else if (Rr == 8) {
-        T2 v[8];
-#pragma unroll
-        for (int r = 0; r < 8; ++r) v[r] = src[r * nb];
-        if (tb) {
-#pragma unroll
-          for (int r = 1; r < 8; ++r) v[r] = twid<T2, INV>(p.tw, r * tb, v[r]);
-        }
-        bfly8<T2, INV>(v);
-#pragma unroll
-        for (int r = 0; r < 8; ++r) dst[r * Ns] = v[r];
-      } else if (Rr == 2) {
-        T2 v0 = src[0], v1 = src[nb];
-        if (tb) v1 = twid<T2, INV>(p.tw, tb, v1);
-        bfly2<T2, INV>(v0, v1);
-        dst[0] = v0; dst[Ns] = v1;
-      } else {  // 3
-        T2 v0 = src[0], v1 = src[nb], v2 = src[2 * nb];
-        if (tb) {
-          v1 = twid<T2, INV>(p.tw, tb, v1);
-          v2 = twid<T2, INV>(p.tw, 2 * tb, v2);
-        }
-        bfly3<T2, INV>(v0, v1, v2);
-        dst[0] = v0; dst[Ns] = v1; dst[2 * Ns] = v2;
-      }
-    }
+    const int nb = p.nbs[s], Ns = p.nss[s];
+    if (s == 0)
+      lines_stage_r<cplx<R>, INV, true>(p.radix[s], a, b, nl, ls, nb, Ns, nb / Ns, p.fnb[s], p.fns[s], p.tw);
+    else
+      lines_stage_r<cplx<R>, INV, false>(p.radix[s], a, b, nl, ls, nb, Ns, nb / Ns, p.fnb[s], p.fns[s], p.tw);
     __syncthreads();
     cplx<R>* tmp = a; a = b; b = tmp;
   }
@@ -344,64 +353,43 @@ struct YGeom {
   FastDiv ftk;               // by tk (the width of an output tile)
 };
 
+template <typename T2, bool INV, int RR, bool FIRST>
+__device__ __forceinline__ void cols_stage(const T2* a, T2* b, int width, const FastDiv& fw, int nb, int Ns, int tws,
+                                           const FastDiv& fns, const T2* tw) {
+  const int total = nb * width;
+  const int sr = nb * width, sd = Ns * width;   // strides between a butterfly's inputs / outputs
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int j = fw.div(t);
+    const int l = t - j * width;
+    const int q = FIRST ? j : fns.div(j);
+    const int jm = j - q * Ns;
+    stage_bfly<T2, INV, RR, FIRST>(a + j * width + l, b + (q * Ns * RR + jm) * width + l, sr, sd, tw, jm * tws);
+  }
+}
+
+template <typename T2, bool INV, bool FIRST>
+__device__ __forceinline__ void cols_stage_r(int Rr, const T2* a, T2* b, int width, const FastDiv& fw, int nb, int Ns,
+                                             int tws, const FastDiv& fns, const T2* tw) {
+  switch (Rr) {
+    case 8: cols_stage<T2, INV, 8, FIRST>(a, b, width, fw, nb, Ns, tws, fns, tw); break;
+    case 4: cols_stage<T2, INV, 4, FIRST>(a, b, width, fw, nb, Ns, tws, fns, tw); break;
+    case 3: cols_stage<T2, INV, 3, FIRST>(a, b, width, fw, nb, Ns, tws, fns, tw); break;
+    default: cols_stage<T2, INV, 2, FIRST>(a, b, width, fw, nb, Ns, tws, fns, tw); break;
+  }
+}
+
 // Stockham FFT along y of the columns of a row-major tile: element y of
 // column l at a[y * width + l].  Threads run over (butterfly, column) with
 // the column fastest, so a warp touches consecutive addresses at every step
 // (no bank conflicts); the butterflies are those of fft_lines.
 template <typename R, bool INV>
 __device__ cplx<R>* fft_cols(cplx<R>* a, cplx<R>* b, int width, const FastDiv& fw, const FftPlan<R>& p) {
-  using T2 = cplx<R>;
   for (int s = 0; s < p.nf; ++s) {
-    const int Rr = p.radix[s];
-    const int nb = p.nbs[s];
-    const int Ns = p.nss[s];
-    const int total = nb * width;
-    const int tws = nb / Ns;
-    const FastDiv fns = p.fns[s];
-    const int sr = nb * width, sd = Ns * width;   // strides between a butterfly's inputs / outputs
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int j = fw.div(t);
-      const int l = t - j * width;
-      const int q = fns.div(j);
-      const int jm = j - q * Ns;
-      const T2* src = a + j * width + l;
-      T2* dst = b + (q * Ns * Rr + jm) * width + l;
-      const int tb = jm * tws;
-      if (Rr == 4) {
-        T2 v0 = src[0], v1 = src[sr], v2 = src[2 * sr], v3 = src[3 * sr];
-        if (tb) {
-          v1 = twid<T2, INV>(p.tw, tb, v1);
-          v2 = twid<T2, INV>(p.tw, 2 * tb, v2);
-          v3 = twid<T2, INV>(p.tw, 3 * tb, v3);
-        }
-        bfly4<T2, INV>(v0, v1, v2, v3);
-        dst[0] = v0; dst[sd] = v1; dst[2 * sd] = v2; dst[3 * sd] = v3;
-      } else if (Rr == 8) {
-        T2 v[8];
-#pragma unroll
-        for (int r = 0; r < 8; ++r) v[r] = src[r * sr];
-        if (tb) {
-#pragma unroll
-          for (int r = 1; r < 8; ++r) v[r] = twid<T2, INV>(p.tw, r * tb, v[r]);
-        }
-        bfly8<T2, INV>(v);
-#pragma unroll
-        for (int r = 0; r < 8; ++r) dst[r * sd] = v[r];
-      } else if (Rr == 2) {
-        T2 v0 = src[0], v1 = src[sr];
-        if (tb) v1 = twid<T2, INV>(p.tw, tb, v1);
-        bfly2<T2, INV>(v0, v1);
-        dst[0] = v0; dst[sd] = v1;
-      } else {  // 3
-        T2 v0 = src[0], v1 = src[sr], v2 = src[2 * sr];
-        if (tb) {
-          v1 = twid<T2, INV>(p.tw, tb, v1);
-          v2 = twid<T2, INV>(p.tw, 2 * tb, v2);
-        }
-        bfly3<T2, INV>(v0, v1, v2);
-        dst[0] = v0; dst[sd] = v1; dst[2 * sd] = v2;
-      }
-    }
+    const int nb = p.nbs[s], Ns = p.nss[s];
+    if (s == 0)
+      cols_stage_r<cplx<R>, INV, true>(p.radix[s], a, b, width, fw, nb, Ns, nb / Ns, p.fns[s], p.tw);
+    else
+      cols_stage_r<cplx<R>, INV, false>(p.radix[s], a, b, width, fw, nb, Ns, nb / Ns, p.fns[s], p.tw);
     __syncthreads();
     cplx<R>* tmp = a; a = b; b = tmp;
   }
