@@ -111,6 +111,9 @@ typedef struct {
   int cumulative_time, inilag;
   int wbase, nenergy, lag_cfl_count, checkpoint_data, checkpoint_nskip;
   int tavg_calc, tavg_nstart, tavg_nend, tavg_nskip;
+  /* TURBINES dyn_theta1, dyn_theta2, dyn_Ct_prime: the schedules to read
+   * with lesgo_gpu_read_turbine_schedule and set per handle */
+  int dyn_theta1, dyn_theta2, dyn_ct_prime;
 } lesgo_run_t;
 
 typedef struct lesgo_handle lesgo_handle_t;
@@ -302,11 +305,34 @@ int lesgo_gpu_tavg_total_time(lesgo_handle_t* h, int id, double* total_time);
  * <path>input_turbines/param.dat.  Host only (no device is touched).
  * Malformed files: LESGO_ERR_ARG with file:line in lesgo_gpu_last_error(NULL);
  * settings whose physics this library leaves out (coriolis_forcing,
- * use_sponge, inflow_type, use_random_force, sgs = .false., dynamic or
- * rotating turbines): LESGO_ERR_UNSUPPORTED.  `log` (may be NULL) receives
+ * use_sponge, inflow_type, use_random_force, sgs = .false., rotating
+ * turbines): LESGO_ERR_UNSUPPORTED.  Time-varying yaw, tilt and Ct' are
+ * reported in run->dyn_*.  `log` (may be NULL) receives
  * the reference's notes on unused blocks and keys. */
 int lesgo_gpu_read_conf(const char* path, int with_turbines, lesgo_params_t* p, lesgo_run_t* run,
                         lesgo_turbine_t* turbines, int max_turbines, char* log, int loglen);
+
+/* ---- turbine control schedules (turbines.f90:500-515; files read by
+ * read_control_files, turbines.f90:872-931) ---------------------------------
+ * which: 0 yaw theta1, 1 tilt theta2 (degrees), 2 Ct'.  `rows` holds nt
+ * rows of 1 + n_turbines values, as the lines of input_turbines/theta1.dat:
+ * the dimensional time, then one value per turbine of the instance.  Every
+ * step each turbine takes the value linearly interpolated at the step's
+ * total_time_dim (binary_search + linear_interp, functions.f90:712-860;
+ * constant beyond the first and last rows).  A yaw or tilt schedule
+ * re-evaluates the actuator-disk nodes and indicator values on the device
+ * each step (turbines_nodes, turbines.f90:275-462).  nt = 0 removes the
+ * schedule.  Times must not decrease; the instance must have turbines. */
+int lesgo_gpu_turbine_schedule(lesgo_handle_t* h, int which, int nt, const double* rows);
+int lesgo_gpu_turbine_schedule_inst(lesgo_handle_t* h, int id, int which, int nt, const double* rows);
+/* Read <path>input_turbines/theta1.dat (which 0), theta2.dat (1) or
+ * Ct_prime.dat (2) for n_turbines disks into rows (max_rows rows of
+ * 1 + n_turbines values); *nt receives the row count.  Host only. */
+int lesgo_gpu_read_turbine_schedule(const char* path, int which, int n_turbines, double* rows, int max_rows,
+                                    int* nt);
+/* Current yaw and tilt (degrees) and Ct' of the instance's turbines, as
+ * the last step used them (the static values before any step). */
+int lesgo_gpu_turbine_controls(lesgo_handle_t* h, int id, double* theta1, double* theta2, double* ct_prime, int n);
 
 /* ---- checkpoint / restart (io.f90:1173-1267 checkpoint; initial.f90:20-380
  * and io.f90:60-96 restart) ------------------------------------------------

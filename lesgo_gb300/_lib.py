@@ -58,7 +58,7 @@ class Run(C.Structure):
         ("Co", C.c_double)] + [(n, C.c_int) for n in ("nsteps", "runtime", "use_cfl_dt")] + [
         ("cfl", C.c_double)] + [(n, C.c_int) for n in (
             "cumulative_time", "inilag", "wbase", "nenergy", "lag_cfl_count", "checkpoint_data", "checkpoint_nskip",
-            "tavg_calc", "tavg_nstart", "tavg_nend", "tavg_nskip")]
+            "tavg_calc", "tavg_nstart", "tavg_nend", "tavg_nskip", "dyn_theta1", "dyn_theta2", "dyn_ct_prime")]
 
 
 # exported symbol -> (restype, argtypes); every function include/lesgo_gpu.h declares
@@ -118,6 +118,10 @@ SIGNATURES = {
     "lesgo_gpu_diag_inst": (_I, [_H, _I, _D, _D, _D, _D]),
     "lesgo_gpu_counters_inst": (_I, [_H, _I, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_turbine_state_inst": (_I, [_H, _I, _D, _D, _D, _I]),
+    "lesgo_gpu_turbine_schedule": (_I, [_H, _I, _I, _D]),
+    "lesgo_gpu_turbine_schedule_inst": (_I, [_H, _I, _I, _I, _D]),
+    "lesgo_gpu_turbine_controls": (_I, [_H, _I, _D, _D, _D, _I]),
+    "lesgo_gpu_read_turbine_schedule": (_I, [C.c_char_p, _I, _I, _D, _I, C.POINTER(_I)]),
     "lesgo_gpu_footprint": (_I, [C.POINTER(Params), _I, C.POINTER(C.c_longlong)]),
     "lesgo_gpu_autotune": (_I, [_H, C.POINTER(_I), C.POINTER(_I)]),
     "lesgo_gpu_diag_log_config": (_I, [_H, _I, _I]),

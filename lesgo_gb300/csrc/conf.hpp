@@ -377,8 +377,7 @@ static void read(const std::string& path, int with_turbines, lesgo_params_t* p, 
   }
   if (!r->sgs) throw ConfError{LESGO_ERR_UNSUPPORTED, "sgs = .false. (no SGS model)"};
   if (seen_turbines) {
-    if (tb.dyn_theta1 || tb.dyn_theta2 || tb.dyn_Ct_prime)
-      throw ConfError{LESGO_ERR_UNSUPPORTED, "time-varying turbine yaw or Ct' (dyn_theta1/dyn_theta2/dyn_Ct_prime)"};
+    r->dyn_theta1 = tb.dyn_theta1; r->dyn_theta2 = tb.dyn_theta2; r->dyn_ct_prime = tb.dyn_Ct_prime;
     if (tb.use_rotation) throw ConfError{LESGO_ERR_UNSUPPORTED, "use_rotation"};
     const std::vector<lesgo_turbine_t> w = place(tb, *p, path + "input_turbines/param.dat");
     if ((int)w.size() > tmax) throw ConfError{LESGO_ERR_ARG, "turbine buffer holds fewer than num_x*num_y disks"};
@@ -387,6 +386,48 @@ static void read(const std::string& path, int with_turbines, lesgo_params_t* p, 
     p->turbines = w.empty() ? nullptr : tbuf;
   }
   if (log) *log = rd.log;
+}
+
+// read_control_files (turbines.f90:872-931): every non-blank line of the
+// file is one row, the dimensional time then one value per turbine
+// (list-directed: blanks or commas between values, D exponents).
+static std::vector<double> read_schedule(const std::string& path, int which, int nturb) {
+  static const char* names[] = {"theta1.dat", "theta2.dat", "Ct_prime.dat"};
+  if (which < 0 || which > 2 || nturb < 1) throw ConfError{LESGO_ERR_ARG, "bad schedule request"};
+  const std::string file = path + "input_turbines/" + names[which];
+  FILE* f = std::fopen(file.c_str(), "r");
+  if (!f) throw ConfError{LESGO_ERR_ARG, "file " + file + " does not exist"};
+  std::vector<double> rows;
+  std::string s;
+  int line = 0;
+  for (int c = 0; c != EOF;) {
+    s.clear();
+    while ((c = std::fgetc(f)) != EOF && c != '\n') s.push_back((char)c);
+    ++line;
+    for (char& ch : s)
+      if (ch == ',' || ch == '\t' || ch == '\r') ch = ' ';
+      else if (ch == 'd' || ch == 'D') ch = 'e';
+    std::vector<double> v;
+    const char* q = s.c_str();
+    char* end;
+    for (;;) {
+      const double x = std::strtod(q, &end);
+      if (end == q) break;
+      v.push_back(x);
+      q = end;
+    }
+    while (*q == ' ') ++q;
+    if (v.empty() && *q == '\0') continue;
+    if ((int)v.size() < 1 + nturb || *q != '\0') {
+      std::fclose(f);
+      throw ConfError{LESGO_ERR_ARG, file + ":" + std::to_string(line) + ": expected the time and " +
+                                         std::to_string(nturb) + " values"};
+    }
+    rows.insert(rows.end(), v.begin(), v.begin() + 1 + nturb);
+  }
+  std::fclose(f);
+  if (rows.empty()) throw ConfError{LESGO_ERR_ARG, file + " holds no rows"};
+  return rows;
 }
 
 }  // namespace conf

@@ -841,6 +841,180 @@ __global__ void k_turb_scatter(TurbDev td, R* fxa, R* fya, R* fza) {
   fza[q] = (R)(fn * td.nhat[3 * s + 2] * ind);
 }
 
+// ---------------------------------------------------------------------------
+// Time-varying turbine controls (turbines.f90:500-515): yaw theta1, tilt
+// theta2 and Ct' interpolated at total_time_dim; with a yaw or tilt schedule
+// the nodes of every disk are re-selected from its search box each step
+// (turbines_nodes, turbines.f90:337-462).
+// ---------------------------------------------------------------------------
+struct TurbDyn {
+  int nturb, dyn_nodes, adm;
+  const int* s_nt;          // [3][nturb] schedule rows (0: none)
+  const int* s_off;         // [3][nturb] offset into s_t / s_v
+  const double* s_t;        // dimensional times
+  const double* s_v;        // values
+  const double* M;          // indicator M of each turbine (ADM correction)
+  double* nhat;             // [nturb*3]     (read by the disk and scatter kernels)
+  double* theta;            // [2][nturb]    current yaw, tilt (degrees)
+  double* ctp;              // [nturb]       current Ct'
+  double* corr;             // [nturb]       1 + 0.25 (1 - M) Ct', or 1
+  const int* tinst;
+  const double* sc;
+  // box nodes
+  const int* dyn_list;      // turbines whose nodes are their search box
+  int ndyn;
+  const int* node_off;      // [nturb+1]
+  const double* box_r;      // [node][3] offset (rx, ry, rz) from the disk centre
+  double* node_ind;         // normalised indicator of each box node (0: not selected)
+  const int* node_turb;     // turbine of each box node
+  const int* tab_off;       // radial table of each turbine (tab_n entries)
+  const double* tab_r;
+  const double* tab_R2;
+  int tab_n;
+  const double* ipar;       // [nturb][4] ell, thk / ell, sqrt(6) / (delta1 / ell), filt_max
+  double cutoff, dx, dy, dz;
+  const long long* win_q;   // window points (union of the boxes)
+  const int* win_coff;      // [nwin+1] candidates of each point, in turbine order
+  const int* win_cand;      // box-node indices
+  int nwin;
+};
+
+// binary_search (functions.f90:811-860) and linear_interp_sa_nocheck
+// (:712-735): v(1) below x(1), v(N) above x(N), else
+// u1 + (xq - x(i)) * (u2 - u1) / (x(i+1) - x(i)).
+__device__ __forceinline__ double sched_interp(const double* x, const double* v, int N, double xq) {
+  int low;
+  if (xq < x[0]) {
+    low = 0;
+  } else if (xq > x[N - 1]) {
+    low = N;
+  } else {
+    low = 1;
+    int high = N;   // one-based, as the reference
+    while (high - low > 1) {
+      const int mid = (low + high) / 2;
+      if (x[mid - 1] > xq) high = mid;
+      else if (x[mid - 1] < xq) low = mid;
+      else { low = mid; break; }
+    }
+  }
+  if (low == 0) return v[0];
+  if (low == N) return v[N - 1];
+  return v[low - 1] + (xq - x[low - 1]) * (v[low] - v[low - 1]) / (x[low] - x[low - 1]);
+}
+
+// One thread per turbine.
+__global__ void k_turb_controls(TurbDyn a) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.nturb) return;
+  const int n = a.nturb;
+  const double t = a.sc[a.tinst[s] * SC_N + SC_TDIM];
+  bool turned = false;
+  for (int w = 0; w < 2; ++w) {
+    const int nt = a.s_nt[w * n + s];
+    if (nt > 0) {
+      a.theta[w * n + s] = sched_interp(a.s_t + a.s_off[w * n + s], a.s_v + a.s_off[w * n + s], nt, t);
+      turned = true;
+    }
+  }
+  if (turned) {   // turbines.f90:343-345
+    const double pi = 3.14159265358979323846;
+    const double t1 = pi * a.theta[s] / 180., t2 = pi * a.theta[n + s] / 180.;
+    a.nhat[3 * s] = -cos(t1) * cos(t2);
+    a.nhat[3 * s + 1] = -sin(t1) * cos(t2);
+    a.nhat[3 * s + 2] = sin(t2);
+  }
+  const int nc = a.s_nt[2 * n + s];
+  if (nc > 0) {
+    const double c = sched_interp(a.s_t + a.s_off[2 * n + s], a.s_v + a.s_off[2 * n + s], nc, t);
+    a.ctp[s] = c;
+    a.corr[s] = a.adm ? (1 + 0.25 * (1 - a.M[s]) * c) : 1.0;   // turbines.f90:579-582
+  }
+}
+
+// The indicator value (turbine_indicator.f90:43-64): the axial window
+// R1 = (erf(s (x/ell + thk/2)) - erf(s (x/ell - thk/2))) / (2 thk) times the
+// radial table interpolated at r/ell (clamped outside it), over ell^3.
+__device__ __forceinline__ double turb_ind_val(const double* r, const double* R2, int N, double ell, double thk,
+                                               double s6d1, double rd, double x) {
+  const double rr = rd / ell, xx = x / ell;
+  int lo = 0, hi = N;   // first index with r[i] > rr
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (r[mid] <= rr) lo = mid + 1;
+    else hi = mid;
+  }
+  double R;
+  if (lo == 0) R = R2[0];
+  else if (lo >= N) R = R2[N - 1];
+  else R = R2[lo - 1] + (rr - r[lo - 1]) * (R2[lo] - R2[lo - 1]) / (r[lo] - r[lo - 1]);
+  const double R1 = 0.5 / thk * (erf(s6d1 * (xx + 0.5 * thk)) - erf(s6d1 * (xx - 0.5 * thk)));
+  return R1 * R / (ell * ell * ell);
+}
+
+// One block per box-node turbine: select its nodes (filt > filter_cutoff * filt_max)
+// and normalise them to integrate to one (turbines.f90:388-437).  The
+// geometry is rounded operation by operation as the reference evaluates it
+// (no fused multiply-adds: r*r - r_norm*r_norm is exactly zero on the axis).
+__global__ void __launch_bounds__(256) k_turb_nodes(TurbDyn a) {
+  __shared__ double sh[256];
+  const int s = a.dyn_list[blockIdx.x];
+  const double n0 = a.nhat[3 * s], n1 = a.nhat[3 * s + 1], n2 = a.nhat[3 * s + 2];
+  const double* tr = a.tab_r + a.tab_off[s];
+  const double* tR = a.tab_R2 + a.tab_off[s];
+  const double ell = a.ipar[4 * s], thk = a.ipar[4 * s + 1], s6d1 = a.ipar[4 * s + 2];
+  const double thr = a.cutoff * a.ipar[4 * s + 3];
+  double acc = 0.0;
+  for (int l = a.node_off[s] + threadIdx.x; l < a.node_off[s + 1]; l += blockDim.x) {
+    const double rx = a.box_r[3 * l], ry = a.box_r[3 * l + 1], rz = a.box_r[3 * l + 2];
+    const double r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz)));
+    const double rn = fabs(__dadd_rn(__dadd_rn(__dmul_rn(rx, n0), __dmul_rn(ry, n1)), __dmul_rn(rz, n2)));
+    const double rd = sqrt(__dsub_rn(__dmul_rn(r, r), __dmul_rn(rn, rn)));
+    const double filt = turb_ind_val(tr, tR, a.tab_n, ell, thk, s6d1, rd, rn);
+    double v = 0.0;
+    if (filt > thr) {
+      v = filt;
+      acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(__dmul_rn(filt, a.dx), a.dy), a.dz));
+    }
+    a.node_ind[l] = v;
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  const double sumA = sh[0];
+  for (int l = a.node_off[s] + threadIdx.x; l < a.node_off[s + 1]; l += blockDim.x) {
+    const double v = a.node_ind[l];
+    if (v != 0.0) a.node_ind[l] = v / sumA;
+  }
+}
+
+// Window point p takes the force of the last turbine (in order) that
+// selected it this step, or zero.
+template <typename R>
+__global__ void k_turb_scatter_dyn(TurbDyn a, const double* f_n, R* fxa, R* fya, R* fza) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.nwin) return;
+  int owner = -1;
+  double ind = 0.0;
+  for (int c = a.win_coff[p]; c < a.win_coff[p + 1]; ++c) {
+    const int l = a.win_cand[c];
+    const double v = a.node_ind[l];
+    if (v != 0.0) { owner = a.node_turb[l]; ind = v; }
+  }
+  const long long q = a.win_q[p];
+  if (owner < 0) {
+    fxa[q] = (R)0; fya[q] = (R)0; fza[q] = (R)0;
+    return;
+  }
+  const double fn = f_n[owner];
+  fxa[q] = (R)(fn * a.nhat[3 * owner] * ind);
+  fya[q] = (R)(fn * a.nhat[3 * owner + 1] * ind);
+  fza[q] = (R)(fn * a.nhat[3 * owner + 2] * ind);
+}
+
 // fza onto the w grid (functions.f90:131-185): fzw(k) = (fza(k-1)+fza(k))/2,
 // k >= 2, fzw(1) = 0, over the turbine footprint columns.
 template <typename R>
@@ -1078,6 +1252,7 @@ __global__ void k_step_begin(StepBeginArgs a) {
     if (f & IF_LAGACC) c[SC_LDT] = c[SC_LDT] + dt;
   }
   c[SC_TIME] = c[SC_TIME] + c[SC_DT];
+  c[SC_TDIM] = c[SC_TDIM] + c[SC_DT] * a.z_i / a.u_star;   // total_time_dim + dt_dim
   if (f & IF_TAACC) c[SC_TAW] = c[SC_TAW] + c[SC_DT];
 }
 

@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <complex>
 #include <cstring>
+#include <array>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -208,15 +209,30 @@ struct TurbineHost {
   std::vector<long long> cols;    // (jy*ld + i) of footprint columns
   std::vector<double> nhat, ctp, corr, dia;
   std::vector<int> tinst;         // instance (slot) of each turbine
+  // control schedules (turbines.f90:500-515): which*n + s -> rows / offset
+  bool dyn_ctl = false, dyn_nodes = false;
+  std::vector<int> s_nt, s_off;
+  std::vector<double> s_t, s_v, theta, Mv;
+  // the turbines of an instance with a yaw or tilt schedule take their whole
+  // search box (turbines.f90:337-361) as node list, re-evaluated every step
+  // on the device; the others keep the nodes selected here
+  std::vector<int> dyn_list;      // box-node turbines
+  std::vector<double> box_r;      // (rx, ry, rz) of each node
+  std::vector<int> node_turb;     // turbine of each node
+  std::vector<int> tab_off;       // indicator table of each turbine
+  std::vector<double> tab_r, tab_R2, ipar;   // ipar: ell, thk, sqrt(6)/delta1, filt_max
+  int tab_n = 0;
+  std::vector<int> win_coff, win_cand;        // candidate box nodes of each window point
 };
 
 // Node lists of the actuator disks of every active instance, with absolute
 // offsets (instance base + level*plane + jy*ld + i).  Indicator tables are
 // cached by (thickness, diameter).
 using IndicatorCache = std::map<std::pair<double, double>, Indicator>;
+using Schedules = std::array<std::vector<double>, 3>;   // rows of theta1, theta2, Ct' (time, one value per turbine)
 
 static TurbineHost turbines_build(const Derived& d, const std::vector<std::vector<lesgo_turbine_t>>& per_inst,
-                                  long long istride, IndicatorCache& cache) {
+                                  const std::vector<Schedules>& sched, long long istride, IndicatorCache& cache) {
   TurbineHost th;
   const auto& P = d.p;
   const double dx = d.dx, dy = d.dy, dz = d.dz;
@@ -225,9 +241,31 @@ static TurbineHost turbines_build(const Derived& d, const std::vector<std::vecto
   const long long plane = (long long)d.ld * d.ny;
   th.node_off.push_back(0);
   std::vector<int> inst_of;
+  std::vector<char> inst_box(per_inst.size(), 0);
+  for (size_t inst = 0; inst < sched.size() && inst < per_inst.size(); ++inst)
+    if (!sched[inst][0].empty() || !sched[inst][1].empty()) th.dyn_nodes = true, inst_box[inst] = 1;
+  for (size_t inst = 0; inst < sched.size(); ++inst)
+    for (int w = 0; w < 3; ++w)
+      if (!sched[inst][w].empty()) th.dyn_ctl = true;
+  std::vector<std::vector<int>> s_nt(3), s_off(3);
+  std::map<std::pair<double, double>, int> tab_of;
   for (size_t inst = 0; inst < per_inst.size(); ++inst) {
     const long long ib = (long long)inst * istride;
+    const int nloc = (int)per_inst[inst].size();
+    int tl = 0;
     for (lesgo_turbine_t t : per_inst[inst]) {
+      // schedule columns of this turbine
+      for (int w = 0; w < 3; ++w) {
+        const std::vector<double>& rows = inst < sched.size() ? sched[inst][w] : std::vector<double>();
+        const int nt = rows.empty() ? 0 : (int)(rows.size() / (1 + nloc));
+        s_nt[w].push_back(nt);
+        s_off[w].push_back((int)th.s_t.size());
+        for (int r = 0; r < nt; ++r) {
+          th.s_t.push_back(rows[(size_t)r * (1 + nloc)]);
+          th.s_v.push_back(rows[(size_t)r * (1 + nloc) + 1 + tl]);
+        }
+      }
+      ++tl;
       t.thk = std::max(t.thk, dx * (double)1.01f);   // turbines.f90:180 (single-precision literal)
       auto key = std::make_pair(t.thk, t.dia);
       if (!cache.count(key)) cache[key] = make_indicator(delta1, delta2, t.thk, t.dia);
@@ -243,6 +281,17 @@ static TurbineHost turbines_build(const Derived& d, const std::vector<std::vecto
       double sumA = 0.0;
       std::vector<long long> q;
       std::vector<double> fv;
+      if (th.dyn_nodes) {
+        auto tk = tab_of.find(key);
+        if (tk == tab_of.end()) {
+          tk = tab_of.emplace(key, (int)th.tab_r.size()).first;
+          th.tab_r.insert(th.tab_r.end(), ind.r.begin(), ind.r.end());
+          th.tab_R2.insert(th.tab_R2.end(), ind.R2.begin(), ind.R2.end());
+          th.tab_n = (int)ind.r.size();
+        }
+        th.tab_off.push_back(tk->second);
+        th.ipar.insert(th.ipar.end(), {ind.ell, ind.thk, ind.s6d1, filt_max});
+      }
       for (int k = 1; k <= d.nz; ++k) {
         if (k > d.nz_tot) continue;
         const double zt = (k - 0.5) * dz;
@@ -257,6 +306,13 @@ static TurbineHost turbines_build(const Derived& d, const std::vector<std::vecto
             else if (j > d.ny) { j2 = ((j + d.ny - 1) % d.ny) + 1; ry = (P.L_y + (j2 - 1) * dy) - t.yloc; }
             else ry = (j - 1) * dy - t.yloc;
             const double rz = zt - t.height;
+            if (inst_box[inst]) {   // every box node; the device selects them each step
+              q.push_back(ib + (long long)k * plane + (j2 - 1) * d.ld + (i2 - 1));
+              fv.push_back(0.0);
+              th.box_r.insert(th.box_r.end(), {rx, ry, rz});
+              th.node_turb.push_back(th.n);
+              continue;
+            }
             const double r = std::sqrt(rx * rx + ry * ry + rz * rz);
             const double r_norm = std::fabs(rx * n1 + ry * n2 + rz * n3);
             const double r_disk = std::sqrt(r * r - r_norm * r_norm);
@@ -265,13 +321,21 @@ static TurbineHost turbines_build(const Derived& d, const std::vector<std::vecto
               q.push_back(ib + (long long)k * plane + (j2 - 1) * d.ld + (i2 - 1));
               fv.push_back(filt);
               sumA += filt * dx * dy * dz;
+              if (th.dyn_nodes) {
+                th.box_r.insert(th.box_r.end(), {rx, ry, rz});
+                th.node_turb.push_back(th.n);
+              }
             }
           }
       }
       for (size_t l = 0; l < q.size(); ++l) {
         th.node_q.push_back(q[l]);
-        th.node_ind.push_back(fv[l] / sumA);
+        th.node_ind.push_back(inst_box[inst] ? 0.0 : fv[l] / sumA);
       }
+      if (inst_box[inst]) th.dyn_list.push_back(th.n);
+      th.theta.push_back(t.theta1);
+      th.theta.push_back(t.theta2);
+      th.Mv.push_back(ind.M);
       th.node_off.push_back((int)th.node_q.size());
       th.nhat.insert(th.nhat.end(), {n1, n2, n3});
       th.ctp.push_back(t.Ct_prime);
@@ -281,6 +345,48 @@ static TurbineHost turbines_build(const Derived& d, const std::vector<std::vecto
       th.tinst.push_back((int)inst);
       ++th.n;
     }
+  }
+  // theta as [which][turbine]
+  {
+    std::vector<double> tt(2 * th.n);
+    for (int s = 0; s < th.n; ++s) { tt[s] = th.theta[2 * s]; tt[th.n + s] = th.theta[2 * s + 1]; }
+    th.theta = tt;
+  }
+  for (int w = 0; w < 3; ++w) {
+    th.s_nt.insert(th.s_nt.end(), s_nt[w].begin(), s_nt[w].end());
+    th.s_off.insert(th.s_off.end(), s_off[w].begin(), s_off[w].end());
+  }
+  if (th.dyn_nodes) {
+    // window: every node point once (first appearance), with the nodes of
+    // all turbines covering it in turbine order; the device gives a point to
+    // the last turbine that selected it this step (assignment order,
+    // turbines.f90:604-606) and zero to unselected points.  Static node
+    // lists take part unchanged (their indicator values are positive).
+    std::unordered_map<long long, int> pos;
+    std::vector<std::vector<int>> cand;
+    for (int s = 0; s < th.n; ++s)
+      for (int l = th.node_off[s]; l < th.node_off[s + 1]; ++l) {
+        auto it = pos.find(th.node_q[l]);
+        if (it == pos.end()) {
+          it = pos.emplace(th.node_q[l], (int)th.win_q.size()).first;
+          th.win_q.push_back(th.node_q[l]);
+          cand.emplace_back();
+        }
+        cand[it->second].push_back(l);
+      }
+    th.win_coff.push_back(0);
+    for (auto& c : cand) {
+      th.win_cand.insert(th.win_cand.end(), c.begin(), c.end());
+      th.win_coff.push_back((int)th.win_cand.size());
+    }
+    std::unordered_map<long long, int> colset;
+    for (long long q : th.win_q) {
+      const long long inst = q / istride;
+      const long long c = inst * istride + (q % istride) % plane;
+      if (!colset.count(c)) { colset[c] = 1; th.cols.push_back(c); }
+    }
+    (void)inst_of;
+    return th;
   }
   // scatter list: within an instance the last turbine in order owns a shared node
   std::unordered_map<long long, std::pair<int, double>> owner;
@@ -312,6 +418,7 @@ struct InstanceSpec {
   double zo;
   uint64_t seed;
   std::vector<lesgo_turbine_t> turbines;
+  Schedules sched;   // control schedules, rows of (time, one value per turbine)
 };
 
 class SolverBase {
@@ -346,6 +453,8 @@ class SolverBase {
   virtual void diag(int id, double* out4) = 0;
   virtual void counters(int id, int* jt, int* jt_total) const = 0;
   virtual void turbine_state(int id, double* udT, double* fn, double* pw, int n) = 0;
+  virtual void turbine_schedule(int id, int which, int nt, const double* rows) = 0;
+  virtual void turbine_controls(int id, double* th1, double* th2, double* ctp, int n) = 0;
   virtual int launches_per_step(int with_sgs) const = 0;
   virtual void profile(int enable) = 0;
   virtual std::string profile_report() = 0;
@@ -907,7 +1016,7 @@ class Solver : public SolverBase {
       const double t = read_sc(slot, SC_TIME);
       td.jt_total = sl.jt_total;
       td.total_time = t;
-      td.total_time_dim = t * d_.p.z_i / d_.p.u_star;
+      td.total_time_dim = read_sc(slot, SC_TDIM);
       td.dt = read_sc(slot, SC_DT);
       td.cfl = d_.p.use_cfl_dt ? d_.p.cfl : dg[2];
       fio::write_time(pre + "total_time.dat", td);
@@ -983,6 +1092,7 @@ class Solver : public SolverBase {
         const fio::TimeDat t = fio::read_time(pre + "total_time.dat");
         sl.jt_total = (int)t.jt_total;
         write_sc(slot, SC_TIME, t.total_time);
+        write_sc(slot, SC_TDIM, t.total_time_dim);
         if (d_.p.use_cfl_dt && t.dt > 0) write_sc(slot, SC_DT, t.dt);
       } else {
         sl.jt_total = 0;
@@ -1241,6 +1351,38 @@ class Solver : public SolverBase {
     }
   }
 
+  void turbine_schedule(int id, int which, int nt, const double* rows) override {
+    const int slot = slot_of(id);
+    InstanceSpec& sp = slots_[slot].spec;
+    const int nloc = (int)sp.turbines.size();
+    if (which < 0 || which > 2 || nt < 0 || (nt > 0 && !rows)) throw Error(LESGO_ERR_ARG, "bad schedule");
+    if (nloc == 0) throw Error(LESGO_ERR_ARG, "instance has no turbines");
+    std::vector<double> v(rows, rows + (size_t)nt * (1 + nloc));
+    for (int r = 1; r < nt; ++r)
+      if (!(v[(size_t)r * (1 + nloc)] >= v[(size_t)(r - 1) * (1 + nloc)]))
+        throw Error(LESGO_ERR_ARG, "schedule times must not decrease");
+    for (double x : v)
+      if (!std::isfinite(x)) throw Error(LESGO_ERR_ARG, "schedule values must be finite");
+    sp.sched[which] = v;
+    rebuild_turbines(-1, -1);
+    CK(cudaStreamSynchronize(st_));
+  }
+  void turbine_controls(int id, double* th1, double* th2, double* ctp, int n) override {
+    const int slot = slot_of(id);
+    const int first = turb_base_.count(slots_[slot].id) ? turb_base_[slots_[slot].id] : 0;
+    const int m = std::min(n, (int)slots_[slot].spec.turbines.size());
+    if (m <= 0 || !th_.n) return;
+    std::vector<double> t(2 * th_.n), c(th_.n);
+    CK(cudaStreamSynchronize(st_));
+    CK(cudaMemcpy(t.data(), tctl_.theta, t.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(c.data(), td_.ctp, c.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int s = 0; s < m; ++s) {
+      if (th1) th1[s] = t[first + s];
+      if (th2) th2[s] = t[th_.n + first + s];
+      if (ctp) ctp[s] = c[first + s];
+    }
+  }
+
   int launches_per_step(int with_sgs) const override {
     auto it = launch_count_.find(with_sgs ? 1 : 0);
     return it == launch_count_.end() ? -1 : it->second;
@@ -1451,7 +1593,8 @@ class Solver : public SolverBase {
     std::vector<double> old(std::max(th_.n, 1), -1.0);
     if (th_.n) CK(cudaMemcpy(old.data(), td_.u_d_T, th_.n * sizeof(double), cudaMemcpyDeviceToHost));
     std::vector<std::vector<lesgo_turbine_t>> per;
-    for (auto& sl : slots_) per.push_back(sl.spec.turbines);
+    std::vector<Schedules> sched;
+    for (auto& sl : slots_) { per.push_back(sl.spec.turbines); sched.push_back(sl.spec.sched); }
     std::vector<double> state;
     for (size_t s = 0; s < slots_.size(); ++s) {
       const int id = slots_[s].id;
@@ -1459,7 +1602,7 @@ class Solver : public SolverBase {
       for (size_t t = 0; t < slots_[s].spec.turbines.size(); ++t)
         state.push_back(it != turb_base_.end() && it->second + (int)t < (int)old.size() && th_.n ? old[it->second + t] : -1.0);
     }
-    th_ = turbines_build(d_, per, kp_.istride, ind_cache_);
+    th_ = turbines_build(d_, per, sched, kp_.istride, ind_cache_);
     turb_base_.clear();
     int base = 0;
     for (auto& sl : slots_) { turb_base_[sl.id] = base; base += (int)sl.spec.turbines.size(); }
@@ -1474,9 +1617,38 @@ class Solver : public SolverBase {
     td_.win_q = upload_vec(th_.win_q);
     td_.win_ind = upload_vec(th_.win_ind);
     td_.nwin = (int)th_.win_q.size();
-    td_.nhat = upload_vec(th_.nhat);
-    td_.ctp = upload_vec(th_.ctp);
-    td_.corr = upload_vec(th_.corr);
+    double* nhat_d = upload_vec(th_.nhat);
+    double* ctp_d = upload_vec(th_.ctp);
+    double* corr_d = upload_vec(th_.corr);
+    double* ind_d = const_cast<double*>(td_.node_ind);
+    td_.nhat = nhat_d; td_.ctp = ctp_d; td_.corr = corr_d;
+    tctl_ = TurbDyn{};
+    tctl_.nturb = th_.n; tctl_.adm = d_.p.adm_correction ? 1 : 0; tctl_.dyn_nodes = th_.dyn_nodes ? 1 : 0;
+    tctl_.s_nt = upload_vec(th_.s_nt); tctl_.s_off = upload_vec(th_.s_off);
+    tctl_.s_t = upload_vec(th_.s_t); tctl_.s_v = upload_vec(th_.s_v);
+    tctl_.M = upload_vec(th_.Mv);
+    tctl_.nhat = nhat_d; tctl_.ctp = ctp_d; tctl_.corr = corr_d;
+    tctl_.theta = upload_vec(th_.theta);
+    tctl_.sc = sc_d_;
+    if (th_.dyn_nodes) {
+      tctl_.dyn_list = upload_vec(th_.dyn_list);
+      tctl_.ndyn = (int)th_.dyn_list.size();
+      tctl_.node_off = td_.node_off;
+      tctl_.box_r = upload_vec(th_.box_r);
+      tctl_.node_ind = ind_d;
+      tctl_.node_turb = upload_vec(th_.node_turb);
+      tctl_.tab_off = upload_vec(th_.tab_off);
+      tctl_.tab_r = upload_vec(th_.tab_r);
+      tctl_.tab_R2 = upload_vec(th_.tab_R2);
+      tctl_.tab_n = th_.tab_n;
+      tctl_.ipar = upload_vec(th_.ipar);
+      tctl_.cutoff = d_.p.filter_cutoff;
+      tctl_.dx = d_.dx; tctl_.dy = d_.dy; tctl_.dz = d_.dz;
+      tctl_.win_q = td_.win_q;
+      tctl_.win_coff = upload_vec(th_.win_coff);
+      tctl_.win_cand = upload_vec(th_.win_cand);
+      tctl_.nwin = (int)th_.win_q.size();
+    }
     td_.dia = upload_vec(th_.dia);
     td_.u_d = alloc<double>(th_.n);
     td_.u_d_T = upload_vec(state);
@@ -1484,6 +1656,7 @@ class Solver : public SolverBase {
     td_.disk = alloc<double>(th_.n);
     td_.tinst = upload_vec(th_.tinst);
     td_.sc = sc_d_;
+    tctl_.tinst = td_.tinst;
     td_.dvol = d_.dx * d_.dy * d_.dz;
     cols_ = upload_vec(th_.cols);
     // the applied-force fields are rewritten only on disk nodes: clear them
@@ -2035,12 +2208,26 @@ class Solver : public SolverBase {
   }
 
   void turb_impl() {
+    if (th_.dyn_ctl) {
+      pre();
+      k_turb_controls<<<(th_.n + 63) / 64, 64, 0, st_>>>(tctl_);
+      post("turbines.controls", 0.0);
+    }
+    if (th_.dyn_nodes && !th_.dyn_list.empty()) {
+      pre();
+      k_turb_nodes<<<(unsigned)th_.dyn_list.size(), 256, 0, st_>>>(tctl_);
+      post("turbines.nodes", (double)th_.node_q.size() * 40.0);
+    }
     pre();
     k_turb_disk<R><<<th_.n, 256, 0, st_>>>(td_, F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], kp_.plane, d_.nz, kp_.istride);
     post("turbines.disk", (double)th_.node_q.size() * (4 * sizeof(R) + 16.0));
     if (td_.nwin > 0) {
       pre();
-      k_turb_scatter<R><<<(td_.nwin + 255) / 256, 256, 0, st_>>>(td_, F_[LESGO_FXA], F_[LESGO_FYA], fza_uv_);
+      if (th_.dyn_nodes)
+        k_turb_scatter_dyn<R><<<(td_.nwin + 255) / 256, 256, 0, st_>>>(tctl_, td_.f_n, F_[LESGO_FXA], F_[LESGO_FYA],
+                                                                      fza_uv_);
+      else
+        k_turb_scatter<R><<<(td_.nwin + 255) / 256, 256, 0, st_>>>(td_, F_[LESGO_FXA], F_[LESGO_FYA], fza_uv_);
       post("turbines.scatter", (double)td_.nwin * (3 * sizeof(R) + 20.0));
       const long long n = (long long)th_.cols.size() * d_.nz;
       pre();
@@ -2096,6 +2283,7 @@ class Solver : public SolverBase {
   double *kxw64_ = nullptr, *kyw64_ = nullptr;
   TurbineHost th_;
   TurbDev td_{};
+  TurbDyn tctl_{};
   IndicatorCache ind_cache_;
   std::map<int, int> turb_base_;
   long long* cols_ = nullptr;
@@ -2496,6 +2684,15 @@ int lesgo_gpu_get_field_inst_async(lesgo_handle_t* h, int id, int f, double* hos
   if (!host) return LESGO_ERR_ARG;
   return guarded(h, [&] { h->s->get_field(id, f, host, lbz, nzhi, false); });
 }
+int lesgo_gpu_turbine_schedule(lesgo_handle_t* h, int which, int nt, const double* rows) {
+  return guarded(h, [&] { h->s->turbine_schedule(h->inst0, which, nt, rows); });
+}
+int lesgo_gpu_turbine_schedule_inst(lesgo_handle_t* h, int id, int which, int nt, const double* rows) {
+  return guarded(h, [&] { h->s->turbine_schedule(id, which, nt, rows); });
+}
+int lesgo_gpu_turbine_controls(lesgo_handle_t* h, int id, double* theta1, double* theta2, double* ct_prime, int n) {
+  return guarded(h, [&] { h->s->turbine_controls(id < 0 ? h->inst0 : id, theta1, theta2, ct_prime, n); });
+}
 int lesgo_gpu_diag_inst(lesgo_handle_t* h, int id, double* rmsdiv, double* ke, double* cfl, double* tau_bot) {
   double out[4] = {0, 0, 0, 0};
   int rc = guarded(h, [&] { h->s->diag(id, out); });
@@ -2614,6 +2811,25 @@ extern "C" int lesgo_gpu_read_conf(const char* path, int with_turbines, lesgo_pa
   } catch (const std::exception& e) {
     g_create_err = e.what();
     return LESGO_ERR_ARG;
+  }
+}
+
+extern "C" int lesgo_gpu_read_turbine_schedule(const char* path, int which, int n_turbines, double* rows,
+                                               int max_rows, int* nt) {
+  if (!path || !nt || (max_rows > 0 && !rows) || max_rows < 0) return LESGO_ERR_ARG;
+  try {
+    const std::vector<double> v = lesgo::conf::read_schedule(path, which, n_turbines);
+    const int n = (int)(v.size() / (1 + n_turbines));
+    if (n > max_rows) {
+      g_create_err = "schedule holds " + std::to_string(n) + " rows, buffer " + std::to_string(max_rows);
+      return LESGO_ERR_ARG;
+    }
+    std::copy(v.begin(), v.end(), rows);
+    *nt = n;
+    return LESGO_OK;
+  } catch (const lesgo::conf::ConfError& e) {
+    g_create_err = e.msg;
+    return e.code;
   }
 }
 

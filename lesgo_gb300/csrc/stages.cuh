@@ -29,10 +29,11 @@ struct KP {
 // replayed step: dt, the AB2 weights tadv1/tadv2 (main.f90:135-144),
 // lagran_dt (sgs_stag_util.f90:72-83), the pressure-RHS scale
 // 1/(nx ny tadv1 dt) (press_stag_array.f90:52), the disk-velocity filter
-// weight of the turbines (turbines.f90:520-530), total_time, and the
-// time-averaging weight pending and its sum (time_average.f90).
+// weight of the turbines (turbines.f90:520-530), total_time, the
+// time-averaging weight pending and its sum (time_average.f90), and
+// total_time_dim (the sum of dt z_i / u_star, main.f90:139-150).
 enum : int {
-  SC_DT = 0, SC_T1, SC_T2, SC_LDT, SC_PS, SC_EPS, SC_TIME, SC_TAW, SC_TAT, SC_DTF, SC_N = 16
+  SC_DT = 0, SC_T1, SC_T2, SC_LDT, SC_PS, SC_EPS, SC_TIME, SC_TAW, SC_TAT, SC_DTF, SC_TDIM, SC_N = 16
 };
 
 // Per-instance step flags: Euler first step (main.f90:273-280), Cs_opt2 =

@@ -100,6 +100,43 @@ def read_conf(path: str, with_turbines: bool = True, max_turbines: int = 4096):
     return kw, rd, log.value.decode()
 
 
+SCHEDULES = {"theta1": 0, "theta2": 1, "Ct_prime": 2}
+
+
+def _which(which) -> int:
+    return SCHEDULES[which] if isinstance(which, str) else int(which)
+
+
+def _set_schedule(check, fn, head, which, rows, nturb):
+    a = np.ascontiguousarray(np.zeros((0, 1 + nturb)) if rows is None else rows, dtype=np.float64)
+    if a.size and (a.ndim != 2 or a.shape[1] != 1 + nturb):
+        raise ValueError("schedule rows need the time and %d values" % nturb)
+    nt = a.shape[0] if a.size else 0
+    check(fn(*head, _which(which), nt, a.ctypes.data_as(C.POINTER(C.c_double))))
+
+
+def _get_controls(lib, check, h, iid, n):
+    t1, t2, c = (np.zeros(max(n, 1)) for _ in range(3))
+    dp = C.POINTER(C.c_double)
+    check(lib.lesgo_gpu_turbine_controls(h, iid, t1.ctypes.data_as(dp), t2.ctypes.data_as(dp),
+                                         c.ctypes.data_as(dp), n))
+    return dict(theta1=t1[:n], theta2=t2[:n], Ct_prime=c[:n])
+
+
+def read_turbine_schedule(path: str, which, n_turbines: int, max_rows: int = 1 << 16) -> np.ndarray:
+    """<path>input_turbines/theta1.dat | theta2.dat | Ct_prime.dat ->
+    rows of (time, one value per turbine) (read_control_files,
+    turbines.f90:872-931)."""
+    lib = L.load()
+    buf = np.zeros((max_rows, 1 + n_turbines))
+    nt = C.c_int()
+    rc = lib.lesgo_gpu_read_turbine_schedule(os.fsencode(path), _which(which), n_turbines,
+                                             buf.ctypes.data_as(C.POINTER(C.c_double)), max_rows, C.byref(nt))
+    if rc != L.LESGO_OK:
+        raise LesgoError(rc, lib.lesgo_gpu_last_error(None).decode())
+    return buf[:nt.value].copy()
+
+
 def footprint_bytes(capacity: int = 1, **kw) -> int:
     """Device bytes a handle of this grid and capacity allocates."""
     lib = L.load()
@@ -298,6 +335,16 @@ class LesgoGPU:
                                                       c.ctypes.data_as(dp), n))
         return dict(u_d_T=a[:n], f_n=b[:n], power=c[:n])
 
+    def turbine_schedule(self, which, rows):
+        """Time-varying yaw (which 0 or "theta1"), tilt (1, "theta2") or Ct'
+        (2, "Ct_prime"): rows of (dimensional time, one value per turbine),
+        as the lines of input_turbines/theta1.dat; None or [] removes it."""
+        _set_schedule(self._check, self._lib.lesgo_gpu_turbine_schedule, (self._h,), which, rows, self.n_turbines)
+
+    def turbine_controls(self):
+        """Current yaw, tilt (degrees) and Ct' of each turbine."""
+        return _get_controls(self._lib, self._check, self._h, -1, self.n_turbines)
+
     def profile(self, enable: bool = True):
         self._check(self._lib.lesgo_gpu_profile(self._h, 1 if enable else 0))
 
@@ -481,6 +528,13 @@ class LesgoBatch:
         self._check(self._lib.lesgo_gpu_turbine_state_inst(self._h, iid, a.ctypes.data_as(dp), b.ctypes.data_as(dp),
                                                            c.ctypes.data_as(dp), n))
         return dict(u_d_T=a[:n], f_n=b[:n], power=c[:n])
+
+    def turbine_schedule(self, iid: int, which, rows):
+        _set_schedule(self._check, self._lib.lesgo_gpu_turbine_schedule_inst, (self._h, iid), which, rows,
+                      self._nturb.get(iid, 0))
+
+    def turbine_controls(self, iid: int):
+        return _get_controls(self._lib, self._check, self._h, iid, self._nturb.get(iid, 0))
 
     def stream_ptr(self) -> int:
         s = C.c_void_p()

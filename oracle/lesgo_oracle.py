@@ -191,6 +191,36 @@ class TurbineFarm:
     adm_correction: bool = True
     T_avg_dim: float = -1.0
     u_d_T0: float = -1.0              # turbines.f90:404-407 (no u_d_T.dat)
+    # control schedules (turbines.f90:500-515): 0 theta1, 1 theta2, 2 Ct' ->
+    # rows (nt, 1 + nloc) of (dimensional time, one value per turbine)
+    sched: dict = field(default_factory=dict)
+
+
+def sched_interp(x, v, xq):
+    """binary_search (functions.f90:811-860) + linear_interp_sa_nocheck
+    (:712-735): v(1) below x(1), v(N) above x(N), else linear between the
+    bracketing samples, u1 + (xq - x(i)) * (u2 - u1) / (x(i+1) - x(i))."""
+    N = len(x)
+    if xq < x[0]:
+        low = 0
+    elif xq > x[N - 1]:
+        low = N
+    else:
+        low, high = 1, N
+        while high - low > 1:
+            mid = (low + high) // 2
+            if x[mid - 1] > xq:
+                high = mid
+            elif x[mid - 1] < xq:
+                low = mid
+            else:
+                low = mid
+                break
+    if low == 0:
+        return float(v[0])
+    if low == N:
+        return float(v[N - 1])
+    return float(v[low - 1] + (xq - x[low - 1]) * (v[low] - v[low - 1]) / (x[low] - x[low - 1]))
 
 
 def _erf(x):
@@ -274,6 +304,7 @@ class Oracle:
         self.jt = 0
         self.jt_total = 0
         self.time = 0.0
+        self.time_dim = 0.0                  # total_time_dim (main.f90:150)
         self.F_LM_MM_init = False
         self.F_QN_NN_init = False
         self._init_wavenumber()
@@ -1012,21 +1043,34 @@ class Oracle:
 
     # ---------------- turbines (turbines.f90:465-638, forcing.f90:79-117) --------------
     def _turbines_init(self, farm: TurbineFarm):
-        """turbines.f90:123-462: node lists and normalised indicator values."""
+        """turbines.f90:123-462: indicator functions, then node lists and
+        normalised indicator values."""
         p = self.p
         self.farm = farm
         self.turb_nodes = []
         dx, dy, dz = p.dx, p.dy, p.dz
-        z_tot = (np.arange(1, p.nz_tot + 1) - 0.5) * dz
-        x, y = self.x, self.y
         for t in farm.turbines:
             # `dx * 1.01`: the literal is default (single) precision
             t.thk = max(t.thk, dx * float(np.float32(1.01)))
         delta1 = farm.alpha1 * math.sqrt(dx ** 2 + dy ** 2 + dz ** 2)
         delta2 = farm.alpha2 * math.sqrt(dx ** 2 + dy ** 2 + dz ** 2)
         for t in farm.turbines:
-            ind_f = IndicatorFunction(delta1, delta2, t.thk, t.dia)
-            t.M = ind_f.M
+            t.ind_f = IndicatorFunction(delta1, delta2, t.thk, t.dia)
+            t.M = t.ind_f.M
+            t.u_d_T = farm.u_d_T0
+            t.u_d = 0.0
+            t.f_n = 0.0
+        self._turbines_nodes()
+
+    def _turbines_nodes(self):
+        """turbines_nodes (turbines.f90:275-462) for the current yaw and tilt."""
+        p = self.p
+        farm = self.farm
+        dx, dy, dz = p.dx, p.dy, p.dz
+        z_tot = (np.arange(1, p.nz_tot + 1) - 0.5) * dz
+        x, y = self.x, self.y
+        for t in farm.turbines:
+            ind_f = t.ind_f
             search_rad = 0.5 * t.dia + 3 * max(farm.alpha1, farm.alpha2) * math.sqrt(dx ** 2 + dy ** 2 + dz ** 2)
             imax = min(int(search_rad / dx + 2), p.nx // 2)
             jmax = min(int(search_rad / dy + 2), p.ny // 2)
@@ -1064,9 +1108,6 @@ class Oracle:
             ind = ind / sumA
             t.ind = ind
             t.nodes = (i2[sel] - 1, j2[sel] - 1, kk[sel])     # zero-based i, j; level k
-            t.u_d_T = farm.u_d_T0
-            t.u_d = 0.0
-            t.f_n = 0.0
 
     def turbines_forcing(self):
         """forcing_applied + turbines_forcing (turbines.f90:465-638)."""
@@ -1079,6 +1120,16 @@ class Oracle:
         w_uv[1:nz] = 0.5 * (self.w[2:nz + 1] + self.w[1:nz])
         w_uv[nz] = w_uv[nz - 1]
         farm = self.farm
+        # time-varying controls (turbines.f90:504-515)
+        nloc = len(farm.turbines)
+        for s, t in enumerate(farm.turbines):
+            for which, attr in ((0, "theta1"), (1, "theta2"), (2, "Ct_prime")):
+                rows = farm.sched.get(which)
+                if rows is not None and len(rows):
+                    rows = np.asarray(rows, dtype=float).reshape(-1, 1 + nloc)
+                    setattr(t, attr, sched_interp(rows[:, 0], rows[:, 1 + s], self.time_dim))
+        if any(farm.sched.get(w) is not None and len(farm.sched.get(w)) for w in (0, 1)):
+            self._turbines_nodes()
         dt_dim = p.dt * p.z_i / p.u_star
         if farm.T_avg_dim > 0.0:
             eps = (dt_dim / farm.T_avg_dim) / (1.0 + dt_dim / farm.T_avg_dim)
@@ -1184,6 +1235,7 @@ class Oracle:
         self.jt_total += 1
         self.jt += 1
         self.time += self.p.dt
+        self.time_dim += self.p.dt * p.z_i / p.u_star
         self.RHSx_f[:] = self.RHSx
         self.RHSy_f[:] = self.RHSy
         self.RHSz_f[:] = self.RHSz
@@ -1438,7 +1490,7 @@ def write_checkpoint(o: "Oracle", prefix: str, ta: Optional["TimeAverage"] = Non
             for n in TAVG_FILE:
                 f.write(fortran_record_bytes(np.ascontiguousarray(ta.acc[n][1:]).tobytes()))
     with open(prefix + "total_time.dat", "w") as f:
-        f.write(" %d %.17E %.17E %.17E %.17E\n" % (o.jt_total, o.time, o.time * p.z_i / p.u_star, p.dt,
+        f.write(" %d %.17E %.17E %.17E %.17E\n" % (o.jt_total, o.time, o.time_dim, p.dt,
                                                   p.cfl if p.use_cfl_dt else o.max_cfl()))
 
 
@@ -1576,6 +1628,7 @@ def read_checkpoint(o: "Oracle", prefix: str, ta: Optional["TimeAverage"] = None
         with open(prefix + "total_time.dat") as f:
             vals = f.read().replace(",", " ").replace("D", "E").split()
         o.jt_total, o.time = int(vals[0]), float(vals[1])
+        o.time_dim = float(vals[2])
         if p.use_cfl_dt:
             p.dt = float(vals[3])                     # io.f90:91-94
     tname = prefix + "tavg.out"

@@ -166,7 +166,7 @@ def test_turbines_block_skipped_without_turbines(built_lib, tmp_path):
     ("CORIOLIS {\ncoriolis_forcing = 1\n}\n", L.LESGO_ERR_UNSUPPORTED, "coriolis_forcing"),
     ("FLOW_COND {\nuse_sponge = .true.\n}\n", L.LESGO_ERR_UNSUPPORTED, "use_sponge"),
     ("MODEL {\nsgs = .false.\n}\n", L.LESGO_ERR_UNSUPPORTED, "sgs"),
-    ("TURBINES {\nnum_x = 1\nnum_y = 1\ndyn_theta1 = T\n}\n", L.LESGO_ERR_UNSUPPORTED, "dyn_theta1"),
+    ("TURBINES {\nnum_x = 1\nnum_y = 1\nuse_rotation = T\n}\n", L.LESGO_ERR_UNSUPPORTED, "use_rotation"),
 ])
 def test_errors(built_lib, tmp_path, text, code, msg):
     with pytest.raises(LesgoError) as ei:
@@ -239,3 +239,38 @@ def test_turbines_from_param_dat(built_lib, tmp_path):
         [(1.0, 0.5, 0.1, 0.1, 0.01, 5.0, 1.33), (1.7, 1.5, 0.1, 0.1, 0.01, 0.0, 1.2)]
     with pytest.raises(LesgoError):
         read_conf(write(tmp_path, "TURBINES {\nnum_x = 3\nnum_y = 1\nread_param = T\n}\n"))
+
+
+def test_dynamic_turbine_flags_and_schedules(built_lib, tmp_path):
+    """dyn_theta1 / dyn_theta2 / dyn_Ct_prime are reported; the control files
+    (read_control_files, turbines.f90:872-931) hold one row per line: the
+    dimensional time and one value per turbine, list-directed."""
+    from lesgo_gb300.solver import read_turbine_schedule
+    text = ("TURBINES {\nnum_x = 2\nnum_y = 1\ndyn_theta1 = .true.\ndyn_Ct_prime = T\n}\n")
+    _, run, _ = read_conf(write(tmp_path, text))
+    assert (run["dyn_theta1"], run["dyn_theta2"], run["dyn_ct_prime"]) == (1, 0, 1)
+    (tmp_path / "input_turbines").mkdir()
+    (tmp_path / "input_turbines" / "theta1.dat").write_text("0.0 0.0 5.0\n\n10.0, 20.0, -5d0\n 25 1.5D1 0\n")
+    rows = read_turbine_schedule(str(tmp_path) + os.sep, "theta1", 2)
+    assert rows.tolist() == [[0.0, 0.0, 5.0], [10.0, 20.0, -5.0], [25.0, 15.0, 0.0]]
+    (tmp_path / "input_turbines" / "Ct_prime.dat").write_text("0.0 1.33\n")
+    with pytest.raises(LesgoError) as ei:
+        read_turbine_schedule(str(tmp_path) + os.sep, 2, 2)
+    assert ei.value.code == L.LESGO_ERR_ARG and "Ct_prime.dat:1" in str(ei.value)
+    with pytest.raises(LesgoError):
+        read_turbine_schedule(str(tmp_path) + os.sep, "theta2", 2)
+
+
+def test_schedule_interpolation_semantics():
+    """binary_search + linear_interp (functions.f90:712-860): clamped to the
+    first / last value outside the table, exact at the samples, linear in
+    between; a repeated time takes the bracket the bisection finds."""
+    from oracle.lesgo_oracle import sched_interp
+    x, v = [0.0, 1.0, 3.0, 3.0, 7.0], [10.0, 20.0, 0.0, 8.0, -4.0]
+    assert sched_interp(x, v, -1.0) == 10.0 and sched_interp(x, v, 8.0) == -4.0
+    assert sched_interp(x, v, 0.5) == 15.0
+    assert sched_interp(x, v, 2.0) == 10.0
+    assert sched_interp(x, v, 1.0) == 20.0
+    assert sched_interp(x, v, 5.0) == 8.0 + 2.0 * (-12.0) / 4.0
+    assert sched_interp(x, v, 7.0) == -4.0
+    assert sched_interp([2.0], [5.0], 2.0) == 5.0 and sched_interp([2.0], [5.0], 9.0) == 5.0
