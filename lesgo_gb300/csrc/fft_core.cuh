@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace lesgo {
 
 template <typename R> struct CplxOf;
@@ -76,6 +78,10 @@ struct FftPlan {
   int nss[kMaxStages];        // sub-transform length Ns entering stage s
   FastDiv fnb[kMaxStages], fns[kMaxStages];
   const cplx<R>* tw;   // tw[t] = exp(-2 pi i t / n), t = 0..n-1
+  // stage twiddles: stage s, butterfly jm, input r (1..radix-1) at
+  // stw[two[s] + jm * (radix - 1) + r - 1] = tw[r * jm * n / (Ns * radix)]
+  const cplx<R>* stw;
+  int two[kMaxStages];
   const cplx<R>* rtw;  // rtw[k] = exp(-2 pi i k / (2n)), k = 0..n (real-transform packing)
 };
 
@@ -161,16 +167,16 @@ __device__ __forceinline__ void bfly(T2* v) {
 // `out(t, j)` the offset of output 0 of a butterfly with q = j / Ns, jm = j
 // % Ns: inputs at src + r * sr, outputs at dst + r * sd (r < RR).  FIRST
 // marks the first stage (Ns = 1: no twiddles, q = j).  The twiddles of
-// butterfly jm are tw[r * jm * tws]; jm = 0 multiplies by tw[0] = 1 exactly,
-// which keeps the warp on one path.
+// butterfly jm are the RR - 1 consecutive entries at `twp` (the stage
+// table); jm = 0 multiplies by 1 exactly, which keeps the warp on one path.
 template <typename T2, bool INV, int RR, bool FIRST>
-__device__ __forceinline__ void stage_bfly(const T2* src, T2* dst, int sr, int sd, const T2* tw, int tb) {
+__device__ __forceinline__ void stage_bfly(const T2* src, T2* dst, int sr, int sd, const T2* twp) {
   T2 v[RR];
 #pragma unroll
   for (int r = 0; r < RR; ++r) v[r] = src[r * sr];
   if (!FIRST) {
 #pragma unroll
-    for (int r = 1; r < RR; ++r) v[r] = twid<T2, INV>(tw, r * tb, v[r]);
+    for (int r = 1; r < RR; ++r) v[r] = twid<T2, INV>(twp, r - 1, v[r]);
   }
   bfly<T2, INV, RR>(v);
 #pragma unroll
@@ -178,26 +184,26 @@ __device__ __forceinline__ void stage_bfly(const T2* src, T2* dst, int sr, int s
 }
 
 template <typename T2, bool INV, int RR, bool FIRST>
-__device__ __forceinline__ void lines_stage(const T2* a, T2* b, int nl, int ls, int nb, int Ns, int tws,
-                                            const FastDiv& fnb, const FastDiv& fns, const T2* tw) {
+__device__ __forceinline__ void lines_stage(const T2* a, T2* b, int nl, int ls, int nb, int Ns,
+                                            const FastDiv& fnb, const FastDiv& fns, const T2* stw) {
   const int total = nl * nb;
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     const int l = fnb.div(t);
     const int j = t - l * nb;
     const int q = FIRST ? j : fns.div(j);
     const int jm = j - q * Ns;
-    stage_bfly<T2, INV, RR, FIRST>(a + l * ls + j, b + l * ls + q * Ns * RR + jm, nb, Ns, tw, jm * tws);
+    stage_bfly<T2, INV, RR, FIRST>(a + l * ls + j, b + l * ls + q * Ns * RR + jm, nb, Ns, stw + jm * (RR - 1));
   }
 }
 
 template <typename T2, bool INV, bool FIRST>
-__device__ __forceinline__ void lines_stage_r(int Rr, const T2* a, T2* b, int nl, int ls, int nb, int Ns, int tws,
-                                              const FastDiv& fnb, const FastDiv& fns, const T2* tw) {
+__device__ __forceinline__ void lines_stage_r(int Rr, const T2* a, T2* b, int nl, int ls, int nb, int Ns,
+                                              const FastDiv& fnb, const FastDiv& fns, const T2* stw) {
   switch (Rr) {
-    case 8: lines_stage<T2, INV, 8, FIRST>(a, b, nl, ls, nb, Ns, tws, fnb, fns, tw); break;
-    case 4: lines_stage<T2, INV, 4, FIRST>(a, b, nl, ls, nb, Ns, tws, fnb, fns, tw); break;
-    case 3: lines_stage<T2, INV, 3, FIRST>(a, b, nl, ls, nb, Ns, tws, fnb, fns, tw); break;
-    default: lines_stage<T2, INV, 2, FIRST>(a, b, nl, ls, nb, Ns, tws, fnb, fns, tw); break;
+    case 8: lines_stage<T2, INV, 8, FIRST>(a, b, nl, ls, nb, Ns, fnb, fns, stw); break;
+    case 4: lines_stage<T2, INV, 4, FIRST>(a, b, nl, ls, nb, Ns, fnb, fns, stw); break;
+    case 3: lines_stage<T2, INV, 3, FIRST>(a, b, nl, ls, nb, Ns, fnb, fns, stw); break;
+    default: lines_stage<T2, INV, 2, FIRST>(a, b, nl, ls, nb, Ns, fnb, fns, stw); break;
   }
 }
 
@@ -209,9 +215,9 @@ __device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FftP
   for (int s = 0; s < p.nf; ++s) {
     const int nb = p.nbs[s], Ns = p.nss[s];
     if (s == 0)
-      lines_stage_r<cplx<R>, INV, true>(p.radix[s], a, b, nl, ls, nb, Ns, nb / Ns, p.fnb[s], p.fns[s], p.tw);
+      lines_stage_r<cplx<R>, INV, true>(p.radix[s], a, b, nl, ls, nb, Ns, p.fnb[s], p.fns[s], p.stw);
     else
-      lines_stage_r<cplx<R>, INV, false>(p.radix[s], a, b, nl, ls, nb, Ns, nb / Ns, p.fnb[s], p.fns[s], p.tw);
+      lines_stage_r<cplx<R>, INV, false>(p.radix[s], a, b, nl, ls, nb, Ns, p.fnb[s], p.fns[s], p.stw + p.two[s]);
     __syncthreads();
     cplx<R>* tmp = a; a = b; b = tmp;
   }
@@ -354,8 +360,8 @@ struct YGeom {
 };
 
 template <typename T2, bool INV, int RR, bool FIRST>
-__device__ __forceinline__ void cols_stage(const T2* a, T2* b, int width, const FastDiv& fw, int nb, int Ns, int tws,
-                                           const FastDiv& fns, const T2* tw) {
+__device__ __forceinline__ void cols_stage(const T2* a, T2* b, int width, const FastDiv& fw, int nb, int Ns,
+                                           const FastDiv& fns, const T2* stw) {
   const int total = nb * width;
   const int sr = nb * width, sd = Ns * width;   // strides between a butterfly's inputs / outputs
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
@@ -363,18 +369,19 @@ __device__ __forceinline__ void cols_stage(const T2* a, T2* b, int width, const 
     const int l = t - j * width;
     const int q = FIRST ? j : fns.div(j);
     const int jm = j - q * Ns;
-    stage_bfly<T2, INV, RR, FIRST>(a + j * width + l, b + (q * Ns * RR + jm) * width + l, sr, sd, tw, jm * tws);
+    stage_bfly<T2, INV, RR, FIRST>(a + j * width + l, b + (q * Ns * RR + jm) * width + l, sr, sd,
+                                   stw + jm * (RR - 1));
   }
 }
 
 template <typename T2, bool INV, bool FIRST>
 __device__ __forceinline__ void cols_stage_r(int Rr, const T2* a, T2* b, int width, const FastDiv& fw, int nb, int Ns,
-                                             int tws, const FastDiv& fns, const T2* tw) {
+                                             const FastDiv& fns, const T2* stw) {
   switch (Rr) {
-    case 8: cols_stage<T2, INV, 8, FIRST>(a, b, width, fw, nb, Ns, tws, fns, tw); break;
-    case 4: cols_stage<T2, INV, 4, FIRST>(a, b, width, fw, nb, Ns, tws, fns, tw); break;
-    case 3: cols_stage<T2, INV, 3, FIRST>(a, b, width, fw, nb, Ns, tws, fns, tw); break;
-    default: cols_stage<T2, INV, 2, FIRST>(a, b, width, fw, nb, Ns, tws, fns, tw); break;
+    case 8: cols_stage<T2, INV, 8, FIRST>(a, b, width, fw, nb, Ns, fns, stw); break;
+    case 4: cols_stage<T2, INV, 4, FIRST>(a, b, width, fw, nb, Ns, fns, stw); break;
+    case 3: cols_stage<T2, INV, 3, FIRST>(a, b, width, fw, nb, Ns, fns, stw); break;
+    default: cols_stage<T2, INV, 2, FIRST>(a, b, width, fw, nb, Ns, fns, stw); break;
   }
 }
 
@@ -387,9 +394,9 @@ __device__ cplx<R>* fft_cols(cplx<R>* a, cplx<R>* b, int width, const FastDiv& f
   for (int s = 0; s < p.nf; ++s) {
     const int nb = p.nbs[s], Ns = p.nss[s];
     if (s == 0)
-      cols_stage_r<cplx<R>, INV, true>(p.radix[s], a, b, width, fw, nb, Ns, nb / Ns, p.fns[s], p.tw);
+      cols_stage_r<cplx<R>, INV, true>(p.radix[s], a, b, width, fw, nb, Ns, p.fns[s], p.stw);
     else
-      cols_stage_r<cplx<R>, INV, false>(p.radix[s], a, b, width, fw, nb, Ns, nb / Ns, p.fns[s], p.tw);
+      cols_stage_r<cplx<R>, INV, false>(p.radix[s], a, b, width, fw, nb, Ns, p.fns[s], p.stw + p.two[s]);
     __syncthreads();
     cplx<R>* tmp = a; a = b; b = tmp;
   }
@@ -417,17 +424,26 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
   const int kx0 = blockIdx.x * g.tk;
   const int li = blockIdx.y;
   const int grp = blockIdx.z;
-  const int tk = min(g.tk, g.K - kx0);
-  // load inputs: column c of input i at row jy
+  const int tkv = min(g.tk, g.K - kx0);
+  // every thread keeps one column c and steps over rows r0, r0 + rstep, ...
+  const int c = threadIdx.x & (g.tk - 1);
+  const int r0 = threadIdx.x >> g.tk_log2;
+  const int rstep = blockDim.x >> g.tk_log2;
+  const bool live = c < tkv;
+  const int kx = kx0 + c;
+#pragma unroll
+  for (int i = 0; i < NIN; ++i) {
+    const auto* src = op.in_plane(grp, i, li) + kx;
+    T2* s = S + i * g.tk + c;
 #pragma unroll 4
-  for (int t = threadIdx.x; t < win * g.ny_in; t += blockDim.x) {
-    const int jy = g.fwin.div(t);
-    const int col = t - jy * win;
-    const int i = col >> g.tk_log2;
-    const int c = col & (g.tk - 1);
-    T2 v = mkc((R)0, (R)0);
-    if (c < tk) v = op.load(grp, i, li, jy, kx0 + c);
-    S[t] = v;
+    for (int jy = r0; jy < g.ny_in; jy += rstep) {
+      T2 v = mkc((R)0, (R)0);
+      if (live) {
+        const auto a = src[(long long)jy * g.K];
+        v = mkc((R)a.x, (R)a.y);
+      }
+      s[jy * win] = v;
+    }
   }
   __syncthreads();
   if (FWD) {
@@ -438,30 +454,32 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
     }
   }
   for (int o = 0; o < NOUT; ++o) {
-    for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
-      const int ky = t >> g.tk_log2, c = t & (g.tk - 1);
-      const int kx = kx0 + c;
+#pragma unroll 2
+    for (int ky = r0; ky < g.ny_out; ky += rstep) {
       T2 acc = mkc((R)0, (R)0);
       const int kin = op.rowmap(ky);
-      if (c < tk && kin >= 0) {
+      if (live && kin >= 0) {
 #pragma unroll
         for (int i = 0; i < NIN; ++i) {
           T2 cf;
-          if (op.coef(grp, o, i, kx, kin, cf)) {
-            T2 s = S[kin * win + i * g.tk + c];
-            acc = cadd(acc, cmul(s, cf));
-          }
+          if (op.coef(grp, o, i, kx, kin, cf)) acc = cadd(acc, cmul(S[kin * win + i * g.tk + c], cf));
         }
       }
-      W0[t] = acc;
+      W0[ky * g.tk + c] = acc;
     }
     __syncthreads();
     T2* res = W0;
     if (INV) res = fft_cols<R, true>(W0, W1, g.tk, g.ftk, pout);
+    if (live) {
+      auto* dst = op.out_plane(grp, o, li) + kx;
+      using OutT = typename std::remove_pointer<decltype(dst)>::type;
 #pragma unroll 4
-    for (int t = threadIdx.x; t < g.tk * g.ny_out; t += blockDim.x) {
-      const int ky = t >> g.tk_log2, c = t & (g.tk - 1);
-      if (c < tk) op.store(grp, o, li, ky, kx0 + c, res[t]);
+      for (int ky = r0; ky < g.ny_out; ky += rstep) {
+        const T2 v = res[ky * g.tk + c];
+        OutT w;
+        w.x = v.x; w.y = v.y;
+        dst[(long long)ky * g.K] = w;
+      }
     }
     __syncthreads();
   }

@@ -1782,13 +1782,25 @@ class Solver : public SolverBase {
       const long double a = -2.0L * kPiL * (long double)k / (long double)(2 * n);
       rtw[k] = mkc((R)cosl(a), (R)sinl(a));
     }
+    // stage tables: butterfly jm's twiddles tw[r * jm * tws], r = 1..radix-1, side by side
+    std::vector<T2> stw;
+    for (int s = 0; s < p.nf; ++s) {
+      p.two[s] = (int)stw.size();
+      const int tws = p.nbs[s] / p.nss[s];
+      if (s == 0) continue;
+      for (int jm = 0; jm < p.nss[s]; ++jm)
+        for (int r = 1; r < p.radix[s]; ++r) stw.push_back(tw[(size_t)r * jm * tws]);
+    }
     T2* dtw = alloc<T2>(n);
     T2* drtw = alloc<T2>(n + 1);
+    T2* dstw = alloc<T2>((long long)stw.size());
     CK(cudaMemcpyAsync(dtw, tw.data(), n * sizeof(T2), cudaMemcpyHostToDevice, st_));
     CK(cudaMemcpyAsync(drtw, rtw.data(), (n + 1) * sizeof(T2), cudaMemcpyHostToDevice, st_));
+    if (!stw.empty()) CK(cudaMemcpyAsync(dstw, stw.data(), stw.size() * sizeof(T2), cudaMemcpyHostToDevice, st_));
     CK(cudaStreamSynchronize(st_));
     p.tw = dtw;
     p.rtw = drtw;
+    p.stw = dstw;
     return p;
   }
 

@@ -236,16 +236,14 @@ struct YOpLin {
   int mul[NOUT][NIN];
   const R *kxw, *kyw, *G1, *G2;
 
-  __device__ __forceinline__ cplx<R> load(int g, int i, int li, int jy, int kx) const {
+  // row 0, column 0 of input i of group g at launch level li (rows K apart)
+  __device__ __forceinline__ const InT* in_plane(int g, int i, int li) const {
     const int inst = fnli.div(li), lv = li - inst * nli;
     const long long plane_idx = (long long)inst * in_inst_levels + in_lev0 + lv * in_levstride;
-    const InT a = in[(long long)(g * NIN + i) * in_fs + (plane_idx * in_rows + jy) * K + kx];
-    return mkc((R)a.x, (R)a.y);
+    return in + (long long)(g * NIN + i) * in_fs + plane_idx * in_rows * K;
   }
-  __device__ __forceinline__ void store(int g, int o, int li, int ky, int kx, cplx<R> v) const {
-    OutT b;
-    b.x = v.x; b.y = v.y;
-    out[(long long)(g * NOUT + o) * out_fs + ((long long)li * out_rows + ky) * K + kx] = b;
+  __device__ __forceinline__ OutT* out_plane(int g, int o, int li) const {
+    return out + (long long)(g * NOUT + o) * out_fs + (long long)li * out_rows * K;
   }
   __device__ __forceinline__ int rowmap(int ko) const {
     const int hs = ny_small / 2;
