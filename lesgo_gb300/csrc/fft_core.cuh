@@ -185,11 +185,13 @@ __device__ __forceinline__ void stage_bfly(const T2* src, T2* dst, int sr, int s
 
 template <typename T2, bool INV, int RR, bool FIRST>
 __device__ __forceinline__ void lines_stage(const T2* a, T2* b, int nl, int ls, int nb, int Ns,
-                                            const FastDiv& fnb, const FastDiv& fns, const T2* stw) {
+                                            const FastDiv& fnl, const FastDiv& fns, const T2* stw) {
+  // the line index runs fastest across threads: with an odd line stride
+  // the stage's loads and stores fall in distinct banks
   const int total = nl * nb;
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
-    const int l = fnb.div(t);
-    const int j = t - l * nb;
+    const int j = fnl.div(t);
+    const int l = t - j * nl;
     const int q = FIRST ? j : fns.div(j);
     const int jm = j - q * Ns;
     stage_bfly<T2, INV, RR, FIRST>(a + l * ls + j, b + l * ls + q * Ns * RR + jm, nb, Ns, stw + jm * (RR - 1));
@@ -198,12 +200,12 @@ __device__ __forceinline__ void lines_stage(const T2* a, T2* b, int nl, int ls, 
 
 template <typename T2, bool INV, bool FIRST>
 __device__ __forceinline__ void lines_stage_r(int Rr, const T2* a, T2* b, int nl, int ls, int nb, int Ns,
-                                              const FastDiv& fnb, const FastDiv& fns, const T2* stw) {
+                                              const FastDiv& fnl, const FastDiv& fns, const T2* stw) {
   switch (Rr) {
-    case 8: lines_stage<T2, INV, 8, FIRST>(a, b, nl, ls, nb, Ns, fnb, fns, stw); break;
-    case 4: lines_stage<T2, INV, 4, FIRST>(a, b, nl, ls, nb, Ns, fnb, fns, stw); break;
-    case 3: lines_stage<T2, INV, 3, FIRST>(a, b, nl, ls, nb, Ns, fnb, fns, stw); break;
-    default: lines_stage<T2, INV, 2, FIRST>(a, b, nl, ls, nb, Ns, fnb, fns, stw); break;
+    case 8: lines_stage<T2, INV, 8, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw); break;
+    case 4: lines_stage<T2, INV, 4, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw); break;
+    case 3: lines_stage<T2, INV, 3, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw); break;
+    default: lines_stage<T2, INV, 2, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw); break;
   }
 }
 
@@ -211,13 +213,13 @@ __device__ __forceinline__ void lines_stage_r(int Rr, const T2* a, T2* b, int nl
 // (line l at a + l*ls).  `b` is scratch of the same shape.  Returns the
 // buffer that holds the result.  All threads of the block must call it.
 template <typename R, bool INV>
-__device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FftPlan<R>& p) {
+__device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FastDiv& fnl, const FftPlan<R>& p) {
   for (int s = 0; s < p.nf; ++s) {
     const int nb = p.nbs[s], Ns = p.nss[s];
     if (s == 0)
-      lines_stage_r<cplx<R>, INV, true>(p.radix[s], a, b, nl, ls, nb, Ns, p.fnb[s], p.fns[s], p.stw);
+      lines_stage_r<cplx<R>, INV, true>(p.radix[s], a, b, nl, ls, nb, Ns, fnl, p.fns[s], p.stw);
     else
-      lines_stage_r<cplx<R>, INV, false>(p.radix[s], a, b, nl, ls, nb, Ns, p.fnb[s], p.fns[s], p.stw + p.two[s]);
+      lines_stage_r<cplx<R>, INV, false>(p.radix[s], a, b, nl, ls, nb, Ns, fnl, p.fns[s], p.stw + p.two[s]);
     __syncthreads();
     cplx<R>* tmp = a; a = b; b = tmp;
   }
@@ -235,7 +237,7 @@ struct XfGeom {
   int rpc;      // rows per CTA
   int ls;       // smem line stride (complex)
   long long out_field_stride;  // complex elements between fields in the output
-  FastDiv fH, fK, fnyrows, frpc;   // by M/2, K, nyrows, rpc
+  FastDiv fH, fK, fnyrows, frpc, fnl;   // by M/2, K, nyrows, rpc, NF * rpc
 };
 
 // Xf: r2c along x for NF fields at once.  Src::load2(n, jy, li, v[NF])
@@ -267,7 +269,7 @@ __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src
     for (int f = 0; f < NF; ++f) A[(f * g.rpc + r) * g.ls + nn] = v[f];
   }
   __syncthreads();
-  T2* Z = fft_lines<R, false>(A, B, nl, g.ls, plan);
+  T2* Z = fft_lines<R, false>(A, B, nl, g.ls, g.fnl, plan);
   const R half = (R)0.5;
   #pragma unroll 4
   for (int t = threadIdx.x; t < nl * g.K; t += blockDim.x) {
@@ -294,7 +296,7 @@ struct XiGeom {
   int rpc;
   int ls;
   long long in_field_stride;
-  FastDiv fH, fM, fnyrows, frpc;   // by M/2, M, nyrows, rpc
+  FastDiv fH, fM, fnyrows, frpc, fnl;   // by M/2, M, nyrows, rpc, NF * rpc
 };
 
 // Xi: c2r along x for NF fields at once, then Dst::store(jy, li, i, vals)
@@ -329,7 +331,7 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
     A[l * g.ls + k] = z;
   }
   __syncthreads();
-  T2* Z = fft_lines<R, true>(A, B, nl, g.ls, plan);
+  T2* Z = fft_lines<R, true>(A, B, nl, g.ls, g.fnl, plan);
   const R* Zr = reinterpret_cast<const R*>(Z);
   #pragma unroll 4
   for (int t = threadIdx.x; t < g.rpc * g.M; t += blockDim.x) {

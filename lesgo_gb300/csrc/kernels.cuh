@@ -537,6 +537,133 @@ __global__ void __launch_bounds__(SEG * COLS) k_thomas(ThomasArgs a) {
   }
 }
 
+// The same solve with each thread's segment (at most LMAX levels) held in
+// registers: all of the segment's loads (right-hand side inputs, pivots)
+// are issued before the recurrences run, and phat is written once.  The
+// arithmetic is k_thomas's, operation for operation.
+template <int SEG, int COLS, int LMAX>
+__global__ void __launch_bounds__(SEG * COLS) k_thomas_r(ThomasArgs a) {
+  __shared__ double2 s_x[SEG][COLS];
+  __shared__ double s_h[SEG][COLS];
+  const int lane = threadIdx.x % COLS, seg = threadIdx.x / COLS;
+  const long long P = (long long)a.ny * a.K;
+  const long long gcol = (long long)blockIdx.x * COLS + lane;
+  const bool live = gcol < P * a.ninst;
+  const int inst = live ? (int)(gcol / P) : 0;
+  const int t = live ? (int)(gcol - inst * P) : 0;
+  const int jy = t / a.K, kx = t - jy * a.K;
+  const int nz = a.nz, n = nz + 1;
+  const double2* Hx = a.Hx + (long long)inst * nz * P;
+  const double2* Hy = a.Hy + (long long)inst * nz * P;
+  const double2* Hz = a.Hz + (long long)inst * nz * P;
+  const double2* Hb = a.Hb + (long long)inst * 2 * P;
+  const double2* Ht = a.Ht + (long long)inst * 2 * P;
+  double2* phat = a.phat + (long long)inst * (nz + 1) * P;
+  const bool nyq = jy == a.ny / 2;
+  const bool mean = kx == 0 && jy == 0;
+  const int L = (n + SEG - 1) / SEG;
+  const int j0 = 1 + seg * L, j1 = min(n, j0 + L - 1);
+  const double c3 = a.idz2;
+  const double kxv = a.kxw[kx], kyv = a.kyw[jy];
+  const bool solve = live && !nyq && !mean;
+  double2 rr[LMAX];
+  double ib[LMAX], gm[LMAX];
+#pragma unroll
+  for (int m = 0; m < LMAX; ++m) {
+    const int j = j0 + m;
+    rr[m] = make_double2(0.0, 0.0);
+    ib[m] = 0.0;
+    gm[m] = 0.0;
+    if (solve && j <= j1) {
+      rr[m] = thomas_rhs(a, Hx, Hy, Hz, Hb, Ht, j, P, t, kxv, kyv);
+      ib[m] = a.ibet[(long long)j * P + t];
+      if (j < n) gm[m] = a.gam[(long long)(j + 1) * P + t];
+    }
+  }
+  // forward map x -> u_{j1} = ut + h x
+  double2 ut = make_double2(0.0, 0.0);
+  double h = 1.0;
+#pragma unroll
+  for (int m = 0; m < LMAX; ++m) {
+    const int j = j0 + m;
+    if (solve && j <= j1) {
+      const double aj = (j == 1) ? 0.0 : (j <= nz ? c3 : -1.0);
+      ut = make_double2((rr[m].x - aj * ut.x) * ib[m], (rr[m].y - aj * ut.y) * ib[m]);
+      h = -aj * ib[m] * h;
+    }
+  }
+  s_x[seg][lane] = ut;
+  s_h[seg][lane] = h;
+  __syncthreads();
+  double2 x = make_double2(0.0, 0.0);
+  for (int s = 0; s < seg; ++s) {
+    const double2 e = s_x[s][lane];
+    const double hs = s_h[s][lane];
+    x = make_double2(e.x + hs * x.x, e.y + hs * x.y);
+  }
+  __syncthreads();
+  // forward re-sweep from the exact input: rr becomes u
+  double2 up = x;
+#pragma unroll
+  for (int m = 0; m < LMAX; ++m) {
+    const int j = j0 + m;
+    if (solve && j <= j1) {
+      const double aj = (j == 1) ? 0.0 : (j <= nz ? c3 : -1.0);
+      up = make_double2((rr[m].x - aj * up.x) * ib[m], (rr[m].y - aj * up.y) * ib[m]);
+      rr[m] = up;
+    }
+  }
+  // backward map y = v_{j1+1} -> v_{j0} = vt + g y
+  double2 vt = make_double2(0.0, 0.0);
+  double g = 1.0;
+#pragma unroll
+  for (int m = LMAX - 1; m >= 0; --m) {
+    const int j = j0 + m;
+    if (solve && j <= j1) {
+      const double gj = gm[m];   // 0 at j = n
+      vt = make_double2(rr[m].x - gj * vt.x, rr[m].y - gj * vt.y);
+      g = -gj * g;
+    }
+  }
+  s_x[seg][lane] = vt;
+  s_h[seg][lane] = g;
+  __syncthreads();
+  double2 y = make_double2(0.0, 0.0);
+  for (int s = SEG - 1; s > seg; --s) {
+    const double2 e = s_x[s][lane];
+    const double gs = s_h[s][lane];
+    y = make_double2(e.x + gs * y.x, e.y + gs * y.y);
+  }
+  if (solve) {
+    double2 vn = y;
+#pragma unroll
+    for (int m = LMAX - 1; m >= 0; --m) {
+      const int j = j0 + m;
+      if (j <= j1) {
+        double2 uj = rr[m];
+        if (j < n) uj = make_double2(uj.x - gm[m] * vn.x, uj.y - gm[m] * vn.y);
+        phat[(j - 1) * P + t] = uj;
+        vn = uj;
+      }
+    }
+  }
+  if (!live) return;
+  if (nyq) {
+    for (int j = j0; j <= j1; ++j) phat[(j - 1) * P + t] = make_double2(0.0, 0.0);
+  } else if (mean && seg == 0) {
+    double2 p = make_double2(0.0, 0.0);
+    phat[t] = p;
+    const double2 hb = Hb[t];
+    p = make_double2(p.x - a.dz * hb.x, p.y - a.dz * hb.y);
+    phat[P + t] = p;
+    for (int jz = 2; jz <= nz; ++jz) {
+      const double2 hz = Hz[(jz - 1) * P + t];
+      p = make_double2(p.x + hz.x * a.dz, p.y + hz.y * a.dz);
+      phat[jz * P + t] = p;
+    }
+  }
+}
+
 // press_stag_array.f90:284-288 dpdz + main.f90:321-326 + forcing.f90:184-243
 // (FUSED: RHSz -= dpdz, project w, boundary conditions) or just dpdz.
 template <typename R, bool FUSED>

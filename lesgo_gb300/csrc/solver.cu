@@ -559,6 +559,7 @@ class Solver : public SolverBase {
     if (const char* b = std::getenv("LESGO_BRANCHES")) branches_allowed_ = std::strcmp(b, "0") != 0;
     if (const char* e = std::getenv("LESGO_XTARGET")) xtarget_ = std::max(256, std::atoi(e));
     if (const char* e = std::getenv("LESGO_YBUDGET")) ybudget_ = (size_t)std::max(8192, std::atoi(e));
+    if (const char* e = std::getenv("LESGO_YTHREADS")) ythreads_ = std::atoi(e) == 128 ? 128 : 256;
     use_graphs_ = graphs_allowed_;
     build_tables();
     CK(cudaStreamSynchronize(st_));
@@ -1907,6 +1908,7 @@ class Solver : public SolverBase {
     g.out_field_stride = (long long)g.nrows * g.K;
     g.fH = FastDiv((unsigned)(M / 2)); g.fK = FastDiv((unsigned)g.K);
     g.fnyrows = FastDiv((unsigned)nyrows); g.frpc = FastDiv((unsigned)g.rpc);
+    g.fnl = FastDiv((unsigned)(NF * g.rpc));
     const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
     auto kern = k_xfwd<R, NF, Src>;
     set_smem(kern, smem);
@@ -1925,6 +1927,7 @@ class Solver : public SolverBase {
     g.in_field_stride = (long long)g.nrows * g.K;
     g.fH = FastDiv((unsigned)(M / 2)); g.fM = FastDiv((unsigned)M);
     g.fnyrows = FastDiv((unsigned)nyrows); g.frpc = FastDiv((unsigned)g.rpc);
+    g.fnl = FastDiv((unsigned)(NF * g.rpc));
     const size_t smem = 2ull * NF * g.rpc * g.ls * sizeof(T2);
     auto kern = k_xinv<R, NF, Dst>;
     set_smem(kern, smem);
@@ -1982,7 +1985,7 @@ class Solver : public SolverBase {
     set_smem(kern, smem);
     dim3 grid((d_.K + tk - 1) / tk, nlev, ngroups);
     pre();
-    kern<<<grid, 256, smem, st_>>>(g, pin, pout, op);
+    kern<<<grid, ythreads_, smem, st_>>>(g, pin, pout, op);
     post(tag, (double)ngroups * nlev * d_.K *
                   ((double)NIN * in_rows * sizeof(InT) + (double)NOUT * out_rows * sizeof(OutT)));
   }
@@ -2180,9 +2183,15 @@ class Solver : public SolverBase {
     ta.dz = d_.dz; ta.idz = 1.0 / d_.dz; ta.idz2 = 1.0 / (d_.dz * d_.dz);
     ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.ninst = kp_.ninst;
     pre();
-    // 16 segments per column when 8 would leave most SMs idle
+    // up to 192 unknowns: 16 segments of at most 12 levels held in
+    // registers; beyond, the looped form (16 segments per column when 8
+    // would leave most SMs idle).  More segments cost FP64 work in the
+    // segment chains, which is what bounds this kernel on GB300.
     const long long ncol = pl_s * kp_.ninst;
-    if (ncol * 8 < 152LL * 1024)
+    const int nu = nz + 1;
+    if (nu <= 192)
+      k_thomas_r<16, 8, 12><<<(unsigned)((ncol + 7) / 8), 128, 0, st_>>>(ta);
+    else if (ncol * 8 < 152LL * 1024)
       k_thomas<16, 16><<<(unsigned)((ncol + 15) / 16), 256, 0, st_>>>(ta);
     else
       k_thomas<8, 32><<<(unsigned)((ncol + 31) / 32), 256, 0, st_>>>(ta);
@@ -2280,6 +2289,7 @@ class Solver : public SolverBase {
   // bytes per block of the y passes
   int xtarget_ = 2048;
   size_t ybudget_ = sizeof(R) == 8 ? 110 * 1024 : 48 * 1024;
+  int ythreads_ = 256;   // y-pass block size (a multiple of the tile width)
   int dlog_cap_ = 0, dlog_every_ = 0;
   long long tacc_stride_ = 0;
   bool tavg_on_ = false;

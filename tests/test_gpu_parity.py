@@ -198,10 +198,11 @@ def test_batch_alone_equals_mixed(built_lib):
         b.close()
 
 
-@pytest.mark.parametrize("grid", [(32, 32, 16), (256, 192, 8)])
+@pytest.mark.parametrize("grid", [(32, 32, 16), (256, 192, 8), (32, 32, 160), (16, 16, 300), (288, 144, 193)])
 def test_pressure_solve_both_segmentations(built_lib, grid):
-    """The Thomas solve runs 16 segments per column on small column counts
-    and 8 on large ones (here 256x192: 24576 columns); both against the
+    """The Thomas solve holds 16 segments of at most 12 levels in registers
+    up to 192 unknowns; beyond, the looped form runs 16 segments per column
+    on small column counts and 8 on large ones; every form against the
     oracle after 2 steps."""
     nx, ny, Nz = grid
     p, o, g = make_pair(nx=nx, ny=ny, Nz=Nz, dyn_init=100)
