@@ -66,6 +66,7 @@ def parse():
                     "B = 128^3 half channel, C = 256x256x192 wind farm with 12 actuator disks")
     ap.add_argument("--val-steps", type=int, default=None)
     ap.add_argument("--val-window", type=int, default=2000)
+    ap.add_argument("--val-no-floor", action="store_true", help="skip the FP64 run-to-run spread (a second FP64 run)")
     ap.add_argument("--only-class", default=None, help="run only the ensemble's instances of one grid class, "
                     "e.g. 96x96x64 (each class is an independent batch: used to profile its launches alone)")
     return ap.parse_args()
@@ -586,7 +587,7 @@ def run_validate(args):
     10 steps over the last `--val-window` steps."""
     import torch
     torch.cuda.set_device(0)
-    from lesgo_gb300.validate import compare, long_run, wind_farm_4x3
+    from lesgo_gb300.validate import compare, ensemble, long_run, wind_farm_4x3
     if args.validate == "B":
         kw = dict(nx=128, ny=128, Nz=128)
         turbines = None
@@ -600,9 +601,17 @@ def run_validate(args):
         turbines = wind_farm_4x3()
         steps = args.val_steps or 3000
     window = min(args.val_window, steps)
-    runs = {prec: long_run(prec, steps, window, 10, 1, turbines, **kw) for prec in ("fp64", "mixed")}
+    # the mixed side averages three realisations (the IC and u scaled by
+    # 1 +- 1e-6); a second FP64 run with u scaled by 1 + 1e-6 gives the
+    # run-to-run spread of the statistics over this window (the noise floor)
+    runs = {"fp64": long_run("fp64", steps, window, 10, 1, turbines, **kw),
+            "mixed": ensemble("mixed", steps, window, 10, 1, turbines, **kw)}
     nz = kw["Nz"] + 1
     r = compare(runs["mixed"], runs["fp64"], nz)
+    if not args.val_no_floor:
+        fl = compare(long_run("fp64", steps, window, 10, 1, turbines, perturb=1e-6, **kw), runs["fp64"], nz)
+        r["fp64_noise_floor"] = {k: v for k, v in fl.items() if k in ("u_linf", "uw_linf", "power_rel")}
+    r["mixed_members"] = runs["mixed"]["members"]
     line = {"validate": args.validate, "grid": [kw["nx"], kw["ny"], kw["Nz"]], "steps": steps, "window": window,
             "nskip": 10, "samples": runs["fp64"]["samples"], "turbines": len(turbines or []),
             "bar": "u_linf <= 0.01 and uw_linf <= 0.01", "pass": r["u_linf"] <= 0.01 and r["uw_linf"] <= 0.01,

@@ -302,6 +302,88 @@ struct InterpArgs {
   KP kp;
 };
 
+// The mixed form's departure point in grid units: a cell index plus a
+// fraction from the displacement -u lagran_dt / dx (below one cell under
+// the Lagrangian CFL), so FP32 keeps the weights to its own precision (an
+// absolute coordinate in FP32 would lose them to cancellation).  The cell
+// and weight rules are cell_indx_w's and trilinear_interp_w's
+// (functions.f90:188-474) in those units: z(m) = m - 1/2, zw(m) = m - 1,
+// the half cell at the wall and lid, periodic wrap in x and y.
+template <typename R>
+__device__ __forceinline__ void interp_fp32(const InterpArgs<R>& a, int i, int j, int k, long long q, long long ib,
+                                            int inst) {
+  const KP& kp = a.kp;
+  const long long P = kp.plane;
+  const int nz = kp.nz;
+  const float ldt = (float)kp.sc[inst * SC_N + SC_LDT];
+  const float cx = ldt * (float)kp.idx, cy = ldt * (float)kp.idy, cz = ldt * (float)kp.idz;
+  float fx, fy, fz;
+  int bz;   // z / dz = bz + fz
+  if (k == 1) {
+    fx = -(float)a.u[q] * cx;
+    fy = -(float)a.v[q] * cy;
+    bz = 0;
+    fz = (kp.lbc == 0) ? 0.0f : 0.5f - 0.25f * (float)a.w[q + P] * cz;
+  } else if (k == nz) {
+    fx = -(float)a.u[q - P] * cx;
+    fy = -(float)a.v[q - P] * cy;
+    if (kp.ubc == 0) { bz = nz - 1; fz = 0.0f; }
+    else { bz = nz - 2; fz = 0.5f - 0.25f * (float)a.w[q - P] * cz; }
+  } else {
+    fx = -0.5f * ((float)a.u[q - P] + (float)a.u[q]) * cx;
+    fy = -0.5f * ((float)a.v[q - P] + (float)a.v[q]) * cy;
+    bz = k - 1;
+    fz = -(float)a.w[q] * cz;
+  }
+  const float flx = floorf(fx), fly = floorf(fy);
+  int ist = i + (int)flx, jst = j + (int)fly;   // zero-based cells, one period at most away
+  if (ist < 0) ist += kp.nx;
+  else if (ist >= kp.nx) ist -= kp.nx;
+  if (jst < 0) jst += kp.ny;
+  else if (jst >= kp.ny) jst -= kp.ny;
+  ist = min(max(ist, 0), kp.nx - 1);   // guards the memory access only
+  jst = min(max(jst, 0), kp.ny - 1);
+  const int ist1 = ist + 1 == kp.nx ? 0 : ist + 1;
+  const int jst1 = jst + 1 == kp.ny ? 0 : jst + 1;
+  const R wx = (R)(fx - flx), wy = (R)(fy - fly);
+  int kst, kst1;
+  float wz;
+  const float zg = (float)bz + fz;   // only compared against the wall and lid cells
+  if (kp.lbc > 0 && zg < 1.0f) {
+    if (zg < 0.5f) { kst = 1; kst1 = 1; wz = 0.0f; }
+    else { kst = 1; kst1 = 2; wz = 2.0f * (((float)bz - 0.5f) + fz); }
+  } else if (kp.ubc > 0 && zg > (float)(nz - 2)) {
+    if (zg > (float)nz - 1.5f) { kst = nz; kst1 = nz; wz = 0.0f; }
+    else { kst = nz - 1; kst1 = nz; wz = 2.0f * ((float)(bz - (nz - 2)) + fz); }
+  } else {
+    const float flz = floorf(fz);
+    kst = bz + (int)flz + 1;
+    // the reference assumes a Lagrangian CFL below one, which keeps kst in
+    // 1..nz-1; the clamp only guards the memory access
+    kst = min(max(kst, 1), nz - 1);
+    kst1 = kst + 1;
+    wz = (float)(bz - (kst - 1)) + fz;
+  }
+  const long long b00 = ib + (long long)jst * kp.ld, b01 = ib + (long long)jst1 * kp.ld;
+  const long long z0 = kst * P, z1 = kst1 * P;
+  const R wzr = (R)wz;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const R* V = a.Fin[f];
+    const R v000 = V[z0 + b00 + ist], v001 = V[z0 + b00 + ist1];
+    const R v010 = V[z0 + b01 + ist], v011 = V[z0 + b01 + ist1];
+    const R v100 = V[z1 + b00 + ist], v101 = V[z1 + b00 + ist1];
+    const R v110 = V[z1 + b01 + ist], v111 = V[z1 + b01 + ist1];
+    const R u1 = v000 + wx * (v001 - v000);
+    const R u2 = v010 + wx * (v011 - v010);
+    const R u3 = v100 + wx * (v101 - v100);
+    const R u4 = v110 + wx * (v111 - v110);
+    const R u5 = u1 + wy * (u2 - u1);
+    const R u6 = u3 + wy * (u4 - u3);
+    a.Fout[f][q] = u5 + wzr * (u6 - u5);
+  }
+}
+
 template <typename R>
 __global__ void k_interp(InterpArgs<R> a) {
   const KP& kp = a.kp;
@@ -314,6 +396,10 @@ __global__ void k_interp(InterpArgs<R> a) {
   const long long q = x_.q;
   const long long ib = x_.inst * kp.istride;
   const int nz = kp.nz;
+  if constexpr (std::is_same<R, float>::value) {
+    interp_fp32(a, i, j, k, q, ib, x_.inst);
+    return;
+  }
   const double ldt = kp.sc[x_.inst * SC_N + SC_LDT], dz = kp.dz;
   const double x = i * kp.dx, y = j * kp.dy;
   auto zc = [&](int kk) { return (kk - 0.5) * dz; };          // grid%z
