@@ -456,6 +456,10 @@ def run_ours(args):
     roof["peak_kind"] = peak_kind
     nc = load_traffic(kname, "ensemble48", "mixed")
     roof["traffic"] = nc["dram_bytes"] if nc else None
+    if nc and "fp64_pipe_pct" in nc:
+        # the pressure solve stays FP64 in the mixed form: bound by the FP64 pipe
+        roof["fp64_pipe_frac"] = nc["fp64_pipe_pct"] / 100.0
+        roof["limiter"] = "FP64 ALU (ncu: FP64 pipe %.0f %% active)" % nc["fp64_pipe_pct"]
     out_forms = {}
     for f, r in res.items():
         v = r["pts"] * r["steps"] * world / (r["ms"] * 1e-3)

@@ -750,6 +750,123 @@ __global__ void __launch_bounds__(SEG * COLS) k_thomas_r(ThomasArgs a) {
   }
 }
 
+// The sequential form: one thread per column sweeps all n levels in the
+// reference's order (forward u_j = (r_j - a_j u_{j-1}) / bet_j, then
+// u_j -= gam_{j+1} u_{j+1}), with half the FP64 work of the segmented form
+// (no segment maps).  Chunks of C levels are double-buffered in registers:
+// the next chunk's loads are in flight while the current one is swept.
+template <int C>
+__device__ __forceinline__ void thomas_fwd_load(const ThomasArgs& a, const double2* Hx, const double2* Hy,
+                                                const double2* Hz, const double2* Hb, const double2* Ht,
+                                                long long P, int t, double kxv, double kyv, int j0, int n,
+                                                double2* rr, double* ib) {
+#pragma unroll
+  for (int m = 0; m < C; ++m) {
+    const int j = j0 + m;
+    if (j <= n) {
+      rr[m] = thomas_rhs(a, Hx, Hy, Hz, Hb, Ht, j, P, t, kxv, kyv);
+      ib[m] = a.ibet[(long long)j * P + t];
+    }
+  }
+}
+
+template <int C>
+__device__ __forceinline__ void thomas_fwd_sweep(double2* phat, long long P, int t, int j0, int n, int nz,
+                                                 double c3, const double2* rr, const double* ib, double2& up) {
+#pragma unroll
+  for (int m = 0; m < C; ++m) {
+    const int j = j0 + m;
+    if (j <= n) {
+      const double aj = (j == 1) ? 0.0 : (j <= nz ? c3 : -1.0);
+      up = make_double2((rr[m].x - aj * up.x) * ib[m], (rr[m].y - aj * up.y) * ib[m]);
+      phat[(j - 1) * P + t] = up;
+    }
+  }
+}
+
+template <int C>
+__device__ __forceinline__ void thomas_bwd_load(const ThomasArgs& a, const double2* phat, long long P, int t, int j1,
+                                                double2* uu, double* gg) {
+#pragma unroll
+  for (int m = 0; m < C; ++m) {
+    const int j = j1 - m;
+    if (j >= 1) {
+      uu[m] = phat[(j - 1) * P + t];
+      gg[m] = a.gam[(long long)(j + 1) * P + t];
+    }
+  }
+}
+
+template <int C>
+__device__ __forceinline__ void thomas_bwd_sweep(double2* phat, long long P, int t, int j1, const double2* uu,
+                                                 const double* gg, double2& vn) {
+#pragma unroll
+  for (int m = 0; m < C; ++m) {
+    const int j = j1 - m;
+    if (j >= 1) {
+      vn = make_double2(uu[m].x - gg[m] * vn.x, uu[m].y - gg[m] * vn.y);
+      phat[(j - 1) * P + t] = vn;
+    }
+  }
+}
+
+template <int C>
+__global__ void __launch_bounds__(128) k_thomas_seq(ThomasArgs a) {
+  const long long P = (long long)a.ny * a.K;
+  const long long gcol = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gcol >= P * a.ninst) return;
+  const int inst = (int)(gcol / P);
+  const int t = (int)(gcol - inst * P);
+  const int jy = t / a.K, kx = t - jy * a.K;
+  const int nz = a.nz, n = nz + 1;
+  const double2* Hx = a.Hx + (long long)inst * nz * P;
+  const double2* Hy = a.Hy + (long long)inst * nz * P;
+  const double2* Hz = a.Hz + (long long)inst * nz * P;
+  const double2* Hb = a.Hb + (long long)inst * 2 * P;
+  const double2* Ht = a.Ht + (long long)inst * 2 * P;
+  double2* phat = a.phat + (long long)inst * (nz + 1) * P;
+  if (jy == a.ny / 2) {
+    for (int j = 1; j <= n; ++j) phat[(j - 1) * P + t] = make_double2(0.0, 0.0);
+    return;
+  }
+  if (kx == 0 && jy == 0) {
+    double2 p = make_double2(0.0, 0.0);
+    phat[t] = p;
+    const double2 hb = Hb[t];
+    p = make_double2(p.x - a.dz * hb.x, p.y - a.dz * hb.y);
+    phat[P + t] = p;
+    for (int jz = 2; jz <= nz; ++jz) {
+      const double2 hz = Hz[(jz - 1) * P + t];
+      p = make_double2(p.x + hz.x * a.dz, p.y + hz.y * a.dz);
+      phat[jz * P + t] = p;
+    }
+    return;
+  }
+  const double c3 = a.idz2;
+  const double kxv = a.kxw[kx], kyv = a.kyw[jy];
+  double2 rA[C], rB[C];
+  double iA[C], iB[C];
+  double2 up = make_double2(0.0, 0.0);
+  thomas_fwd_load<C>(a, Hx, Hy, Hz, Hb, Ht, P, t, kxv, kyv, 1, n, rA, iA);
+  for (int j0 = 1; j0 <= n; j0 += 2 * C) {
+    thomas_fwd_load<C>(a, Hx, Hy, Hz, Hb, Ht, P, t, kxv, kyv, j0 + C, n, rB, iB);
+    thomas_fwd_sweep<C>(phat, P, t, j0, n, nz, c3, rA, iA, up);
+    thomas_fwd_load<C>(a, Hx, Hy, Hz, Hb, Ht, P, t, kxv, kyv, j0 + 2 * C, n, rA, iA);
+    thomas_fwd_sweep<C>(phat, P, t, j0 + C, n, nz, c3, rB, iB, up);
+  }
+  // u_n stays; levels n-1 .. 1
+  double2 vn = up;
+  double2 uA[C], uB[C];
+  double gA[C], gB[C];
+  thomas_bwd_load<C>(a, phat, P, t, n - 1, uA, gA);
+  for (int j1 = n - 1; j1 >= 1; j1 -= 2 * C) {
+    thomas_bwd_load<C>(a, phat, P, t, j1 - C, uB, gB);
+    thomas_bwd_sweep<C>(phat, P, t, j1, uA, gA, vn);
+    thomas_bwd_load<C>(a, phat, P, t, j1 - 2 * C, uA, gA);
+    thomas_bwd_sweep<C>(phat, P, t, j1 - C, uB, gB, vn);
+  }
+}
+
 // press_stag_array.f90:284-288 dpdz + main.f90:321-326 + forcing.f90:184-243
 // (FUSED: RHSz -= dpdz, project w, boundary conditions) or just dpdz.
 template <typename R, bool FUSED>

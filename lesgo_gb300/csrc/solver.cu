@@ -560,6 +560,8 @@ class Solver : public SolverBase {
     if (const char* e = std::getenv("LESGO_XTARGET")) xtarget_ = std::max(256, std::atoi(e));
     if (const char* e = std::getenv("LESGO_YBUDGET")) ybudget_ = (size_t)std::max(8192, std::atoi(e));
     if (const char* e = std::getenv("LESGO_YTHREADS")) ythreads_ = std::atoi(e) == 128 ? 128 : 256;
+    if (const char* e = std::getenv("LESGO_THOMAS"))
+      thomas_mode_ = std::strcmp(e, "seq") == 0 ? 1 : std::strcmp(e, "seg") == 0 ? 2 : 0;
     use_graphs_ = graphs_allowed_;
     build_tables();
     CK(cudaStreamSynchronize(st_));
@@ -2183,18 +2185,22 @@ class Solver : public SolverBase {
     ta.dz = d_.dz; ta.idz = 1.0 / d_.dz; ta.idz2 = 1.0 / (d_.dz * d_.dz);
     ta.nz = nz; ta.ny = ny; ta.K = d_.K; ta.ninst = kp_.ninst;
     pre();
-    // up to 192 unknowns: 16 segments of at most 12 levels held in
-    // registers; beyond, the looped form (16 segments per column when 8
-    // would leave most SMs idle).  More segments cost FP64 work in the
-    // segment chains, which is what bounds this kernel on GB300.
+    // The FP64 pipe bounds this solve on GB300.  With enough columns (a
+    // batch; measured: 17280 columns 20 % and 45056 columns 51 % faster
+    // than segmented) one thread sweeps each column in order, which does
+    // half the FP64 work of the segmented forms; with fewer columns (one
+    // 128^3 instance: 8320) the segmented forms keep the SMs busy: 16
+    // segments held in registers up to 192 unknowns, the looped form beyond.
+    // LESGO_THOMAS=seq|seg forces a form.
     const long long ncol = pl_s * kp_.ninst;
     const int nu = nz + 1;
-    if (nu <= 192)
+    const bool seq = thomas_mode_ == 1 || (thomas_mode_ == 0 && ncol >= 12288);
+    if (seq)
+      k_thomas_seq<8><<<(unsigned)((ncol + 127) / 128), 128, 0, st_>>>(ta);
+    else if (nu <= 192)
       k_thomas_r<16, 8, 12><<<(unsigned)((ncol + 7) / 8), 128, 0, st_>>>(ta);
-    else if (ncol * 8 < 152LL * 1024)
-      k_thomas<16, 16><<<(unsigned)((ncol + 15) / 16), 256, 0, st_>>>(ta);
     else
-      k_thomas<8, 32><<<(unsigned)((ncol + 31) / 32), 256, 0, st_>>>(ta);
+      k_thomas<16, 16><<<(unsigned)((ncol + 15) / 16), 256, 0, st_>>>(ta);
     post("press.thomas", (double)pl_s * kp_.ninst * (4.0 * nz + 1.0) * sizeof(double2));
     // p, i kx p, i ky p at levels 1..nz-1; p at levels 0 and nz (phat holds nz+1 planes per instance)
     // p at levels 0 and nz on the second stream
@@ -2290,6 +2296,7 @@ class Solver : public SolverBase {
   int xtarget_ = 2048;
   size_t ybudget_ = sizeof(R) == 8 ? 110 * 1024 : 48 * 1024;
   int ythreads_ = 256;   // y-pass block size (a multiple of the tile width)
+  int thomas_mode_ = 0;   // 0 by column count, 1 sequential, 2 segmented
   int dlog_cap_ = 0, dlog_every_ = 0;
   long long tacc_stride_ = 0;
   bool tavg_on_ = false;

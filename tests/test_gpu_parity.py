@@ -198,12 +198,13 @@ def test_batch_alone_equals_mixed(built_lib):
         b.close()
 
 
-@pytest.mark.parametrize("grid", [(32, 32, 16), (256, 192, 8), (32, 32, 160), (16, 16, 300), (288, 144, 193)])
+@pytest.mark.parametrize("grid", [(32, 32, 16), (32, 32, 160), (16, 16, 300), (256, 192, 8), (256, 96, 40)])
 def test_pressure_solve_both_segmentations(built_lib, grid):
-    """The Thomas solve holds 16 segments of at most 12 levels in registers
-    up to 192 unknowns; beyond, the looped form runs 16 segments per column
-    on small column counts and 8 on large ones; every form against the
-    oracle after 2 steps."""
+    """The Thomas solve: on few columns 16 segments per column, held in
+    registers up to 192 unknowns (32x32x16, 32x32x160) and looped beyond
+    (16x16x300); from 12288 columns one thread per column sweeping in order
+    with double-buffered chunks (256x192x8, 256x96x40: partial chunks).
+    Every form against the oracle after 2 steps."""
     nx, ny, Nz = grid
     p, o, g = make_pair(nx=nx, ny=ny, Nz=Nz, dyn_init=100)
     for _ in range(2):
