@@ -487,7 +487,9 @@ __global__ void k_interp(InterpArgs<R> a) {
 // input in the reference's order: u_j = (r_j - a_j u_{j-1}) / bet_j forward,
 // u_j = u_j - gam_{j+1} u_{j+1} backward.
 // ---------------------------------------------------------------------------
-// SEG segments per column, COLS columns per block (SEG * COLS = 256 threads).
+// SEG segments per column, COLS columns per block (SEG * COLS threads).
+// The host picks among this looped form, the register-held k_thomas_r and
+// the sequential k_thomas_seq (below) by column count and unknowns.
 
 struct ThomasArgs {
   const double2 *Hx, *Hy, *Hz;   // levels 1..nz at index level-1, [inst][nz][P]
