@@ -41,6 +41,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -94,8 +95,10 @@ class Clocks:
     def __init__(self, idx: int):
         self.idx = idx
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{idx}.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else f"/tmp/lesgo_clocks_{os.getpid()}.csv"
+        # the raw samples go to $LESGO_CLOCKS_DIR when set (kept), else a temporary file
+        d = os.environ.get("LESGO_CLOCKS_DIR")
+        self.path = (os.path.join(d, f"clocks_rank{idx}.csv") if d and os.path.isdir(d)
+                     else os.path.join(tempfile.gettempdir(), f"lesgo_clocks_{os.getpid()}_{idx}.csv"))
 
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
