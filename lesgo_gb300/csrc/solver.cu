@@ -572,6 +572,7 @@ class Solver : public SolverBase {
     for (auto& r : prof_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
     for (void* p : allocs_) cudaFree(p);
+    for (void* p : turb_allocs_) cudaFree(p);
     for (auto& e : ev_)
       if (e) cudaEventDestroy(e);
     for (auto& e : ring_ev_)
@@ -1592,6 +1593,12 @@ class Solver : public SolverBase {
   }
 
   void rebuild_turbines(int moved_to, int moved_from) {
+    // Nothing queued or captured may read the disk arrays replaced below:
+    // both streams drain and the captured steps (which hold the arrays and
+    // the disk counts as launch parameters) are dropped before they are freed.
+    CK(cudaStreamSynchronize(st_));
+    CK(cudaStreamSynchronize(st2_));
+    graphs_clear();
     // carry the disk-velocity state (u_d_T) of surviving turbines across the rebuild
     std::vector<double> old(std::max(th_.n, 1), -1.0);
     if (th_.n) CK(cudaMemcpy(old.data(), td_.u_d_T, th_.n * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1609,65 +1616,85 @@ class Solver : public SolverBase {
     turb_base_.clear();
     int base = 0;
     for (auto& sl : slots_) { turb_base_[sl.id] = base; base += (int)sl.spec.turbines.size(); }
+    for (void* q : turb_allocs_) cudaFree(q);
+    turb_allocs_.clear();
+    td_ = TurbDev{};
+    tctl_ = TurbDyn{};
+    cols_ = nullptr;
     kp_.turbines = th_.n > 0 ? 1 : 0;
     if (!kp_.turbines) return;
     if (!fza_uv_) fza_uv_ = alloc<R>(nfield_);
     td_.nturb = th_.n;
-    td_.node_off = upload_vec(th_.node_off);
-    td_.node_q = upload_vec(th_.node_q);
-    td_.node_ind = upload_vec(th_.node_ind);
-    td_.win_turb = upload_vec(th_.win_turb);
-    td_.win_q = upload_vec(th_.win_q);
-    td_.win_ind = upload_vec(th_.win_ind);
+    td_.node_off = tupload(th_.node_off);
+    td_.node_q = tupload(th_.node_q);
+    td_.node_ind = tupload(th_.node_ind);
+    td_.win_turb = tupload(th_.win_turb);
+    td_.win_q = tupload(th_.win_q);
+    td_.win_ind = tupload(th_.win_ind);
     td_.nwin = (int)th_.win_q.size();
-    double* nhat_d = upload_vec(th_.nhat);
-    double* ctp_d = upload_vec(th_.ctp);
-    double* corr_d = upload_vec(th_.corr);
+    double* nhat_d = tupload(th_.nhat);
+    double* ctp_d = tupload(th_.ctp);
+    double* corr_d = tupload(th_.corr);
     double* ind_d = const_cast<double*>(td_.node_ind);
     td_.nhat = nhat_d; td_.ctp = ctp_d; td_.corr = corr_d;
     tctl_ = TurbDyn{};
     tctl_.nturb = th_.n; tctl_.adm = d_.p.adm_correction ? 1 : 0; tctl_.dyn_nodes = th_.dyn_nodes ? 1 : 0;
-    tctl_.s_nt = upload_vec(th_.s_nt); tctl_.s_off = upload_vec(th_.s_off);
-    tctl_.s_t = upload_vec(th_.s_t); tctl_.s_v = upload_vec(th_.s_v);
-    tctl_.M = upload_vec(th_.Mv);
+    tctl_.s_nt = tupload(th_.s_nt); tctl_.s_off = tupload(th_.s_off);
+    tctl_.s_t = tupload(th_.s_t); tctl_.s_v = tupload(th_.s_v);
+    tctl_.M = tupload(th_.Mv);
     tctl_.nhat = nhat_d; tctl_.ctp = ctp_d; tctl_.corr = corr_d;
-    tctl_.theta = upload_vec(th_.theta);
+    tctl_.theta = tupload(th_.theta);
     tctl_.sc = sc_d_;
     if (th_.dyn_nodes) {
-      tctl_.dyn_list = upload_vec(th_.dyn_list);
+      tctl_.dyn_list = tupload(th_.dyn_list);
       tctl_.ndyn = (int)th_.dyn_list.size();
       tctl_.node_off = td_.node_off;
-      tctl_.box_r = upload_vec(th_.box_r);
+      tctl_.box_r = tupload(th_.box_r);
       tctl_.node_ind = ind_d;
-      tctl_.node_turb = upload_vec(th_.node_turb);
-      tctl_.tab_off = upload_vec(th_.tab_off);
-      tctl_.tab_r = upload_vec(th_.tab_r);
-      tctl_.tab_R2 = upload_vec(th_.tab_R2);
+      tctl_.node_turb = tupload(th_.node_turb);
+      tctl_.tab_off = tupload(th_.tab_off);
+      tctl_.tab_r = tupload(th_.tab_r);
+      tctl_.tab_R2 = tupload(th_.tab_R2);
       tctl_.tab_n = th_.tab_n;
-      tctl_.ipar = upload_vec(th_.ipar);
+      tctl_.ipar = tupload(th_.ipar);
       tctl_.cutoff = d_.p.filter_cutoff;
       tctl_.dx = d_.dx; tctl_.dy = d_.dy; tctl_.dz = d_.dz;
       tctl_.win_q = td_.win_q;
-      tctl_.win_coff = upload_vec(th_.win_coff);
-      tctl_.win_cand = upload_vec(th_.win_cand);
+      tctl_.win_coff = tupload(th_.win_coff);
+      tctl_.win_cand = tupload(th_.win_cand);
       tctl_.nwin = (int)th_.win_q.size();
     }
-    td_.dia = upload_vec(th_.dia);
-    td_.u_d = alloc<double>(th_.n);
-    td_.u_d_T = upload_vec(state);
-    td_.f_n = alloc<double>(th_.n);
-    td_.disk = alloc<double>(th_.n);
-    td_.tinst = upload_vec(th_.tinst);
+    td_.dia = tupload(th_.dia);
+    td_.u_d = talloc<double>(th_.n);
+    td_.u_d_T = tupload(state);
+    td_.f_n = talloc<double>(th_.n);
+    td_.disk = talloc<double>(th_.n);
+    td_.tinst = tupload(th_.tinst);
     td_.sc = sc_d_;
     tctl_.tinst = td_.tinst;
     td_.dvol = d_.dx * d_.dy * d_.dz;
-    cols_ = upload_vec(th_.cols);
+    cols_ = tupload(th_.cols);
     // the applied-force fields are rewritten only on disk nodes: clear them
     for (int f : {LESGO_FXA, LESGO_FYA, LESGO_FZA})
       CK(cudaMemsetAsync(F_[f], 0, nfield_ * sizeof(R), st_));
     CK(cudaMemsetAsync(fza_uv_, 0, nfield_ * sizeof(R), st_));
-    graphs_clear();
+    CK(cudaStreamSynchronize(st_));
     (void)moved_to; (void)moved_from;
+  }
+  // Device arrays of the disks, freed at the next rebuild.
+  template <typename T>
+  T* talloc(long long n) {
+    void* p = nullptr;
+    CK(cudaMalloc(&p, std::max<long long>(n, 1) * sizeof(T)));
+    turb_allocs_.push_back(p);
+    CK(cudaMemsetAsync(p, 0, std::max<long long>(n, 1) * sizeof(T), st_));
+    return (T*)p;
+  }
+  template <typename T>
+  T* tupload(const std::vector<T>& v) {
+    T* p = talloc<T>((long long)v.size());
+    if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st_));
+    return p;
   }
   void graphs_clear() {
     for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
@@ -2313,6 +2340,7 @@ class Solver : public SolverBase {
   TurbineHost th_;
   TurbDev td_{};
   TurbDyn tctl_{};
+  std::vector<void*> turb_allocs_;
   IndicatorCache ind_cache_;
   std::map<int, int> turb_base_;
   long long* cols_ = nullptr;

@@ -129,3 +129,31 @@ def test_total_time_dim_through_checkpoint(built_lib, tmp_path):
     assert np.array_equal(a.turbine_controls()["theta1"], c.turbine_controls()["theta1"])
     a.close()
     c.close()
+
+
+@pytest.mark.gpu
+def test_disks_leaving_a_batch_leave_no_forcing(built_lib):
+    """The last instance with disks leaves and another joins at the same
+    instance count: its steps carry no disk forcing (the captured steps of
+    the earlier disk layout are dropped at every rebuild) and equal its run
+    alone."""
+    from lesgo_gb300.solver import LesgoBatch, LesgoGPU
+    from test_gpu_parity import _farm
+    ts, _ = _farm(2, 1)
+    b = LesgoBatch(capacity=2, **KW)
+    a = b.add(1e-4, 51, turbines=ts)
+    k = b.add(2e-4, 52)
+    b.step(3)
+    b.remove(a)
+    c = b.add(3e-4, 53)
+    b.step(3)
+    for iid, zo, seed, n in ((k, 2e-4, 52, 6), (c, 3e-4, 53, 3)):
+        # k moved into the slot the disks' instance held
+        assert not np.any(b.get(iid, "fxa")) and not np.any(b.get(iid, "fza")), iid
+        g = LesgoGPU(zo=zo, **KW)
+        g.init_ic(seed)
+        g.step(n)
+        for f in ("u", "v", "w"):
+            assert np.array_equal(b.get(iid, f)[1:g.nz], g.get(f)[1:g.nz]), (iid, f)
+        g.close()
+    b.close()
