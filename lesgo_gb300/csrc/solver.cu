@@ -1285,6 +1285,10 @@ class Solver : public SolverBase {
     if (every < 1 || capacity < 1) throw Error(LESGO_ERR_ARG, "diag log: every and capacity must be >= 1");
     if (!diag_part_) { diag_part_ = alloc<double>(4 * 152 * 7); diag_out_ = alloc<double>(8); }
     if (capacity != dlog_cap_) {
+      if (dlog_) {   // queued samples may still write the old ring
+        CK(cudaStreamSynchronize(st_));
+        release(dlog_);
+      }
       dlog_ = alloc<double>((long long)cap_ * capacity * 6);
       dlog_cap_ = capacity;
     }
@@ -1747,6 +1751,13 @@ class Solver : public SolverBase {
     CK(cudaMemsetAsync(p, 0, std::max<long long>(n, 1) * sizeof(T), st_));
     allocs_.push_back(p);
     return (T*)p;
+  }
+  // Free one allocation of alloc() (the caller makes sure no queued work uses it).
+  void release(void* p) {
+    auto it = std::find(allocs_.begin(), allocs_.end(), p);
+    if (it == allocs_.end()) return;
+    cudaFree(*it);
+    allocs_.erase(it);
   }
   double* staging(long long n) {
     if (n > staging_n_) {
