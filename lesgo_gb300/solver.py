@@ -137,6 +137,17 @@ def read_turbine_schedule(path: str, which, n_turbines: int, max_rows: int = 1 <
     return buf[:nt.value].copy()
 
 
+def conf_turbine_schedules(path: str, run: dict, n_turbines: int) -> dict:
+    """The control schedules a lesgo.conf asks for (run["dyn_theta1"] etc.
+    from read_conf), read from <path>input_turbines/: {which: rows}.  Pass
+    each to turbine_schedule(which, rows)."""
+    out = {}
+    for which, flag in (("theta1", "dyn_theta1"), ("theta2", "dyn_theta2"), ("Ct_prime", "dyn_ct_prime")):
+        if run.get(flag):
+            out[which] = read_turbine_schedule(path, which, n_turbines)
+    return out
+
+
 def footprint_bytes(capacity: int = 1, **kw) -> int:
     """Device bytes a handle of this grid and capacity allocates."""
     lib = L.load()

@@ -259,6 +259,10 @@ def test_dynamic_turbine_flags_and_schedules(built_lib, tmp_path):
     assert ei.value.code == L.LESGO_ERR_ARG and "Ct_prime.dat:1" in str(ei.value)
     with pytest.raises(LesgoError):
         read_turbine_schedule(str(tmp_path) + os.sep, "theta2", 2)
+    from lesgo_gb300.solver import conf_turbine_schedules
+    (tmp_path / "input_turbines" / "Ct_prime.dat").write_text("0.0 1.33 1.2\n5.0 1.0 1.1\n")
+    sch = conf_turbine_schedules(str(tmp_path) + os.sep, run, 2)
+    assert sorted(sch) == ["Ct_prime", "theta1"] and sch["Ct_prime"].shape == (2, 3)
 
 
 def test_schedule_interpolation_semantics():
