@@ -9,8 +9,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "liblesgo_gpu.so")
 SOURCES = [os.path.join(HERE, "csrc", "solver.cu")]
-DEPS = SOURCES + [os.path.join(HERE, "csrc", f) for f in ("fft_core.cuh", "stages.cuh", "kernels.cuh")] + [
-    os.path.join(ROOT, "include", "lesgo_gpu.h")]
+DEPS = SOURCES + sorted(os.path.join(HERE, "csrc", f) for f in os.listdir(os.path.join(HERE, "csrc"))
+                        if f.endswith((".cuh", ".hpp"))) + [os.path.join(ROOT, "include", "lesgo_gpu.h")]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
