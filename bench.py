@@ -50,6 +50,8 @@ sys.path.insert(0, ROOT)
 METRIC = "grid-pt-steps/s on 1 GB300: FP32 batched vs FP64 plain at <=1% profile error"
 UNIT = "grid-pt-steps/s"
 WORKLOAD = dict(nx=128, ny=128, Nz=128, dyn_init=5, cs_count=5)
+WORKLOAD_DESC = ("48 independent half-channel LES instances of uneven grids (48^3, 64^3, 96x96x64, 128x64x64), "
+                 "z0 log-uniform in [1e-5, 1e-3], own IC seeds")
 
 
 def parse():
@@ -268,10 +270,8 @@ def time_batched(args, torch):
     from lesgo_gb300.solver import LesgoGPU
     inst = batch_instances()
     batches = make_batches("mixed")
-    warm = max(args.warmup, 6)
-    warm = (warm + 4) // 5 * 5
+    warm, steps = timed_steps(args)
     step_all(batches, warm)
-    steps = max(5, (args.steps + 4) // 5 * 5)
     ms = timed_on_device(torch, batches, lambda: step_all(batches, steps))
     pts = sum(g[0] * g[1] * g[2] * len(ids) for g, ids, _ in batches)
     launches = sum((4 * b.launches_per_step(False) + b.launches_per_step(True)) for _, _, b in batches) * steps // 5
@@ -381,32 +381,58 @@ def time_e2e(args, torch):
     return dict(value=n * n * n * steps / dt, h2d=nbytes, d2h=nbytes)
 
 
-def oracle_sample(steps=1):
-    """The FP64 oracle port on every grid class of the ensemble (one instance
-    each, one warm step, then `steps` timed steps, the first of which
-    carries the dynamic SGS update), threaded FFTs on all host cores.
-    Returns grid-pt-steps/s and the description of the sample."""
+def class_counts():
+    """Instances per grid class in the ensemble."""
+    counts = {}
+    for g, _, _ in batch_instances():
+        counts[g] = counts.get(g, 0) + 1
+    return counts
+
+
+def timed_steps(args):
+    """Warm-up and timed step counts of both arms: the timed region starts
+    at a multiple of 5 and spans whole multiples of 5 steps, so every arm
+    sees the same phase of the every-5-steps dynamic SGS update."""
+    warm = (max(args.warmup, 6) + 4) // 5 * 5
+    steps = max(5, (args.steps + 4) // 5 * 5)
+    return warm, steps
+
+
+def oracle_sample(warm, steps):
+    """The FP64 oracle port, one instance of each grid class of the ensemble
+    in turn (dyn_init = cs_count = 5 like the GPU arm), `warm` untimed steps,
+    then `steps` timed steps, threaded FFTs on all host cores.  The
+    ensemble's rate weights each class by its instance count: sum over
+    classes of instances x points / sum of instances x seconds per step
+    (the 48 instances run one at a time).  Returns the rate, the cores and
+    the sample's description."""
     from oracle.lesgo_oracle import Oracle, Params
     cores = os.cpu_count() or 1
-    pts, secs = 0, 0.0
-    for g in BATCH_GRIDS:
-        o = Oracle(Params(nx=g[0], ny=g[1], Nz=g[2], dyn_init=1, cs_count=2, zo=1e-4))
+    counts = class_counts()
+    work, secs = 0.0, 0.0
+    for k, g in enumerate(BATCH_GRIDS):
+        if g not in counts:
+            continue
+        o = Oracle(Params(nx=g[0], ny=g[1], Nz=g[2], dyn_init=5, cs_count=5, zo=1e-4))
         o.workers = cores
-        o.set_ic(1)
-        o.step()
+        o.set_ic(5000 + k)
+        for _ in range(warm):
+            o.step()
         t0 = time.perf_counter()
         for _ in range(steps):
             o.step()
-        secs += time.perf_counter() - t0
-        pts += g[0] * g[1] * g[2] * steps
-    sample = (f"{steps} step(s) of one instance of each grid class "
-              f"({', '.join('x'.join(map(str, g)) for g in BATCH_GRIDS)}) of the FP64 oracle port "
-              f"(numpy + scipy.fft, {cores} workers), one with the dynamic SGS update")
-    return pts / secs, cores, sample
+        per_step = (time.perf_counter() - t0) / steps
+        work += counts[g] * g[0] * g[1] * g[2]
+        secs += counts[g] * per_step
+    sample = (f"one instance of each grid class "
+              f"({', '.join('x'.join(map(str, g)) + ' x' + str(counts.get(g, 0)) for g in BATCH_GRIDS)}) of the "
+              f"FP64 oracle port (numpy + scipy.fft, {cores} workers), {warm} warm-up + {steps} timed steps each "
+              f"(dynamic SGS update every 5 steps, as the GPU arm), weighted by the class's instance count")
+    return work / secs, cores, sample
 
 
 def cpu_baseline(args):
-    value, cores, sample = oracle_sample(2)
+    value, cores, sample = oracle_sample(5, 5)
     return dict(value=value, unit=UNIT, cores=cores, kind="port", sample=sample)
 
 
@@ -490,10 +516,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (f64 pressure solve, wall law, step constants)",
         "data": "synthetic (seeded log-law + noise IC)",
-        "config": {"workload": "48 independent half-channel LES instances of uneven grids (48^3, 64^3, 96x96x64, "
-                               "128x64x64), z0 log-uniform in [1e-5, 1e-3], own IC seeds; mixed form "
-                               "(FP32 bulk, FP64 Poisson), one batch per grid class, graph-replayed steps, "
-                               "autotuned tiles",
+        "config": {"workload": WORKLOAD_DESC + "; mixed form (FP32 bulk, FP64 Poisson), one batch per grid "
+                               "class, graph-replayed steps, autotuned tiles",
                    "instances": batched["instances"], "grids": batched["grids"],
                    "sgs": "Lagrangian scale-dependent, every 5 steps", "dt": 2e-4,
                    "vs_fp64_plain_one_at_a_time": batched["ratio_vs_fp64_one_at_a_time"],
@@ -527,24 +551,30 @@ def load_traffic(kernel, grid, form):
 
 
 def run_reference(args):
-    """The reference arm: the FP64 oracle port on the host cores, on a bounded
-    sample of the same ensemble (the Fortran reference needs gfortran, MPI and
-    FFTW, absent here)."""
+    """The reference arm: the FP64 oracle port on the host cores, on the same
+    ensemble, SGS phase, warm-up and timed step counts as the GPU arm, one
+    instance per grid class standing for its class (the Fortran reference
+    needs gfortran, MPI and FFTW, absent on the GPU machine)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    steps = max(1, min(args.steps, 2))
-    value, cores, sample = oracle_sample(steps)
-    ms = sum(g[0] * g[1] * g[2] for g in BATCH_GRIDS) * steps / value * 1e3 / steps
+    warm, steps = timed_steps(args)
+    t0 = time.perf_counter()
+    value, cores, sample = oracle_sample(warm, steps)
+    pts = sum(g[0] * g[1] * g[2] * n for g, n in class_counts().items())
+    ms = pts / value * 1e3
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded log-law + noise IC)",
-        "config": {"workload": "48 independent half-channel LES instances of uneven grids (48^3, 64^3, 96x96x64, "
-                               "128x64x64); the reference computes in FP64 one instance at a time",
-                   "grids": [list(g) for g in BATCH_GRIDS]},
+        "config": {"workload": WORKLOAD_DESC + "; the reference computes in FP64 one instance at a time",
+                   "instances": sum(class_counts().values()),
+                   "grids": {"x".join(map(str, g)): n for g, n in class_counts().items()},
+                   "sgs": "Lagrangian scale-dependent, every 5 steps", "dt": 2e-4,
+                   "wall_s": time.perf_counter() - t0},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample + "; the Fortran reference needs gfortran + MPI + FFTW, absent"},
+                         "sample": sample + "; the Fortran reference needs gfortran + MPI + FFTW, absent on the "
+                                            "GPU box (probed)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -209,7 +209,9 @@ int lesgo_gpu_tridag_array(lesgo_handle_t* h, const double* a, const double* b, 
  * The first call on a device looks up that array's address (make it
  * outside stream capture).  Calls share the array: calls whose GPU work
  * overlaps race.  Launches on `stream` (NULL: default stream) and returns
- * when done; errors are described by lesgo_gpu_last_error(NULL). */
+ * when done; LESGO_ERR_NUMERIC on a zero pivot.  After a nonzero return,
+ * lesgo_gpu_last_error(NULL) describes the failure; a successful call does
+ * not clear that message, so read it only right after a failed call. */
 int lesgo_gpu_tridag_array_noalloc(const double* a, const double* b, const double* c, const double* r,
                                    double* u, int lh, int ny, int n, void* stream);
 

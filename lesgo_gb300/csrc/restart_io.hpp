@@ -82,7 +82,24 @@ static void write_record(FILE* f, const std::vector<Part>& parts) {
   } while (left > 0);
 }
 
-// Read the next record; false at end of file.
+// Bytes from the current position to the end of the file.
+static int64_t bytes_left(FILE* f) {
+  const long at = std::ftell(f);
+  if (at < 0 || std::fseek(f, 0, SEEK_END) != 0) return INT64_MAX;
+  const long end = std::ftell(f);
+  std::fseek(f, at, SEEK_SET);
+  return end < at ? 0 : (int64_t)(end - at);
+}
+
+static int32_t bswap32(int32_t v) {
+  const uint32_t u = (uint32_t)v;
+  return (int32_t)((u >> 24) | ((u >> 8) & 0xFF00u) | ((u << 8) & 0xFF0000u) | (u << 24));
+}
+
+// Read the next record; false at end of file.  A record whose length marker
+// only makes sense byte-swapped was written big-endian (the reference's
+// WRITE_ENDIAN=BIG build, convert='BIG_ENDIAN'): it is rejected by name
+// rather than read as a huge length.
 static bool read_record(FILE* f, std::vector<char>& out) {
   out.clear();
   bool first = true;
@@ -93,6 +110,13 @@ static bool read_record(FILE* f, std::vector<char>& out) {
       throw IoError{"truncated record"};
     }
     const int64_t len = lead < 0 ? -(int64_t)lead : lead;
+    const int64_t left = bytes_left(f);
+    if (len + 4 > left) {
+      const int32_t sw = bswap32(lead);
+      const int64_t slen = sw < 0 ? -(int64_t)sw : sw;
+      if (slen + 4 <= left) throw IoError{"big-endian checkpoint (WRITE_ENDIAN=BIG) not supported"};
+      throw IoError{"truncated record"};
+    }
     const size_t at = out.size();
     out.resize(at + (size_t)len);
     if (len > 0 && std::fread(out.data() + at, 1, (size_t)len, f) != (size_t)len) throw IoError{"truncated record"};

@@ -234,3 +234,23 @@ def test_gpu_tavg_restart_matches_oracle(built_lib, tmp_path):
         a = g2.tavg_get(name)[:o.p.nz - 1, :, :o.p.nx]
         assert np.max(np.abs(a - ref)) <= 1e-10 * max(np.max(np.abs(ref)), 1e-30), name
     g2.close()
+
+
+@pytest.mark.gpu
+def test_gpu_rejects_big_endian_checkpoint(built_lib, tmp_path):
+    """The reference's WRITE_ENDIAN=BIG build writes every record marker and
+    value big-endian; the reader names that instead of reading a byte-swapped
+    record length."""
+    from lesgo_gb300.solver import LesgoError, LesgoGPU
+    g = LesgoGPU(**BASE)
+    ld = 2 * (BASE["nx"] // 2 + 1)
+    nzf = BASE["Nz"] + 1
+    payload = np.zeros(11 * ld * BASE["ny"] * nzf, dtype=">f8").tobytes()
+    rec = struct.pack(">i", len(payload)) + payload + struct.pack(">i", len(payload))
+    pre = str(tmp_path) + os.sep
+    with open(pre + "vel.out", "wb") as f:
+        f.write(rec)
+    with pytest.raises(LesgoError) as ei:
+        g.checkpoint_read(pre)
+    assert "big-endian" in str(ei.value)
+    g.close()

@@ -43,6 +43,36 @@ def test_noalloc_matches_allocating_entry_point_twice(built_lib):
         assert np.array_equal(out[~m], ref[~m])       # untouched entries identical (sentinel)
 
 
+def test_noalloc_zero_pivot_then_good_call_on_callers_stream(built_lib):
+    import torch
+    from lesgo_gb300 import _lib
+    from lesgo_gb300.solver import LesgoGPU
+    lib = _lib.load()
+    g = LesgoGPU(nx=32, ny=32, Nz=16)
+    s = torch.cuda.Stream()
+
+    def on_stream(a, b, c, r, u, lh, ny, n):
+        return lib.lesgo_gpu_tridag_array_noalloc(C.c_void_p(a), C.c_void_p(b), C.c_void_p(c), C.c_void_p(r),
+                                                  C.c_void_p(u), lh, ny, n, C.c_void_p(s.cuda_stream))
+
+    # a zero pivot is reported as LESGO_ERR_NUMERIC ...
+    a, b, c, r = tridiag_case(lh=5, ny=4, n=6, seed=3)
+    b[0] = 0.0
+    rcs = []
+    gpu_solve(lambda *args: rcs.append(on_stream(*args)), a, b, c, r)
+    assert rcs == [_lib.LESGO_ERR_NUMERIC]
+    assert b"zero pivot" in lib.lesgo_gpu_last_error(None)
+    # ... and the flag left set by that call does not fail the next good one
+    a, b, c, r = tridiag_case(lh=33, ny=64, n=40, seed=4)
+    ref = gpu_solve(g.tridag_array, a, b, c, r)
+    rcs.clear()
+    out = gpu_solve(lambda *args: rcs.append(on_stream(*args)), a, b, c, r)
+    assert rcs == [_lib.LESGO_OK]
+    m = solved_entries(out, ref)
+    err = np.max(np.abs(out[m] - ref[m])) / np.max(np.abs(ref[m]))
+    assert err <= TOL, err
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(built_lib):
     from lesgo_gb300 import _lib
     lib = _lib.load()
