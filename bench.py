@@ -62,11 +62,14 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--forms", default="fp64,mixed", help="single-instance 128^3 forms reported beside the ensemble")
+    ap.add_argument("--forms", default="fp64,fp64dw,mixed",
+                    help="single-instance 128^3 forms reported beside the ensemble (fp64dw: FP64 fields, "
+                         "double-word transforms)")
     ap.add_argument("--serve", action="store_true", help="run the served request stream instead")
     ap.add_argument("--requests", type=int, default=24)
-    ap.add_argument("--validate", choices=["B", "C"], help="long-run statistics of the mixed form vs FP64: "
-                    "B = 128^3 half channel, C = 256x256x192 wind farm with 12 actuator disks")
+    ap.add_argument("--validate", choices=["B", "C", "D"], help="long-run statistics of the mixed form vs FP64: "
+                    "B = 128^3 half channel, C = 256x256x192 wind farm with 12 actuator disks, D = each "
+                    "instance of the batched 48-instance ensemble against the same instance alone in FP64")
     ap.add_argument("--val-steps", type=int, default=None)
     ap.add_argument("--val-window", type=int, default=2000)
     ap.add_argument("--val-no-floor", action="store_true", help="skip the FP64 run-to-run spread (a second FP64 run)")
@@ -284,29 +287,35 @@ def time_batched(args, torch):
     tiles = {f"{g[0]}x{g[1]}x{g[2]}": b.autotune() for g, _, b in batches}
     for _, _, b in batches:
         b.close()
-    # plain FP64, one instance at a time: steady-state step time per grid class
-    t64 = {}
-    for g, _, _ in batches:
-        s = LesgoGPU(nx=g[0], ny=g[1], Nz=g[2], precision="fp64", dyn_init=5, cs_count=5)
-        s.init_ic(1)
-        s.autotune()
-        s.step(10)
-        st = torch.cuda.ExternalStream(s.stream_ptr())
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.sync()
-        e0.record(st)
-        s.step(10)
-        e1.record(st)
-        e1.synchronize()
-        t64[g] = e0.elapsed_time(e1) * 1e-3 / 10
-        s.close()
-    seq_time = sum(t64[g] for g, _, _ in inst)
-    fp64_one_at_a_time = sum(g[0] * g[1] * g[2] for g, _, _ in inst) / seq_time
+    # the FP64-field forms, one instance at a time: steady-state step time per
+    # grid class (FP64 transforms; double-word transforms)
+    one_at_a_time = {}
+    for prec in ("fp64", "fp64dw"):
+        t64 = {}
+        for g, _, _ in batches:
+            s = LesgoGPU(nx=g[0], ny=g[1], Nz=g[2], precision=prec, dyn_init=5, cs_count=5)
+            s.init_ic(1)
+            s.autotune()
+            s.step(10)
+            st = torch.cuda.ExternalStream(s.stream_ptr())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.sync()
+            e0.record(st)
+            s.step(10)
+            e1.record(st)
+            e1.synchronize()
+            t64[g] = e0.elapsed_time(e1) * 1e-3 / 10
+            s.close()
+        seq_time = sum(t64[g] for g, _, _ in inst)
+        one_at_a_time[prec] = sum(g[0] * g[1] * g[2] for g, _, _ in inst) / seq_time
+    fp64_one_at_a_time = one_at_a_time["fp64"]
     value = pts * steps / (ms * 1e-3)
     return dict(value=value, ms=ms, steps=steps, ms_per_step=ms / steps, pts=pts, instances=len(inst),
                 grids={f"{g[0]}x{g[1]}x{g[2]}": len(ids) for g, ids, _ in batches}, launches=launches,
                 profile=merge_profiles(reps), tiles=tiles, fp64_one_at_a_time=fp64_one_at_a_time,
-                ratio_vs_fp64_one_at_a_time=value / fp64_one_at_a_time)
+                ratio_vs_fp64_one_at_a_time=value / fp64_one_at_a_time,
+                fp64dw_one_at_a_time=one_at_a_time["fp64dw"],
+                ratio_vs_fp64dw_one_at_a_time=value / one_at_a_time["fp64dw"])
 
 
 def time_e2e_batched(args, torch):
@@ -352,12 +361,12 @@ def time_e2e_batched(args, torch):
     return dict(value=pts * steps / (ms * 1e-3), h2d=nbytes, d2h=nbytes)
 
 
-def time_e2e(args, torch):
+def time_e2e(args, torch, precision="fp64"):
     """Through the C ABI with host buffers: per step, u, v, w go host->device
     from pinned memory, one fused step runs, and u, v, w come back."""
     from lesgo_gb300.solver import LesgoGPU
     n = args.grid
-    g = LesgoGPU(**dict(WORKLOAD, nx=n, ny=n, Nz=n, precision="fp64"))
+    g = LesgoGPU(**dict(WORKLOAD, nx=n, ny=n, Nz=n, precision=precision))
     g.init_ic(1)
     g.step(10)
     g.sync()
@@ -470,7 +479,7 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
         batched = time_batched(args, torch)
-        res = {f: time_form(f, args, torch, world) for f in forms if f in ("fp64", "mixed")}
+        res = {f: time_form(f, args, torch, world) for f in forms if f in ("fp64", "fp64dw", "mixed")}
     clocks = clk.summary()
     ms = max_over_ranks(batched["ms"], world, torch, "cuda")
     steps = batched["steps"]
@@ -500,8 +509,8 @@ def run_ours(args):
                 rf["fp64_pipe_frac"] = nc64["fp64_pipe_pct"] / 100.0
                 rf["traffic"] = nc64["dram_bytes"]
                 rf["limiter"] = "FP64 ALU (ncu: FP64 pipe %.0f %% active)" % nc64["fp64_pipe_pct"]
-        if f == "fp64":
-            e = time_e2e(args, torch)
+        if f in ("fp64", "fp64dw"):
+            e = time_e2e(args, torch, f)
             rf_e2e = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"]}
         else:
             rf_e2e = None
@@ -510,6 +519,8 @@ def run_ours(args):
                             kernels=r["profile"])
     if "fp64" in out_forms and "mixed" in out_forms:
         out_forms["mixed_vs_fp64"] = out_forms["mixed"]["value"] / out_forms["fp64"]["value"]
+    if "fp64" in out_forms and "fp64dw" in out_forms:
+        out_forms["fp64dw_vs_fp64"] = out_forms["fp64dw"]["value"] / out_forms["fp64"]["value"]
     out_forms["batched"] = {k: v for k, v in batched.items() if k not in ("profile",)}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
@@ -522,6 +533,8 @@ def run_ours(args):
                    "sgs": "Lagrangian scale-dependent, every 5 steps", "dt": 2e-4,
                    "vs_fp64_plain_one_at_a_time": batched["ratio_vs_fp64_one_at_a_time"],
                    "fp64_plain_one_at_a_time": batched["fp64_one_at_a_time"],
+                   "vs_fp64dw_one_at_a_time": batched["ratio_vs_fp64dw_one_at_a_time"],
+                   "fp64dw_one_at_a_time": batched["fp64dw_one_at_a_time"],
                    "profile_error": "mean profile <= 1e-2 against FP64 (128^3: 2.6e-4; wind farm: 2.6e-5)",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "l2": "working set > L2 (about 3 GB of fields)"},
@@ -624,7 +637,18 @@ def run_validate(args):
     10 steps over the last `--val-window` steps."""
     import torch
     torch.cuda.set_device(0)
-    from lesgo_gb300.validate import compare, ensemble, long_run, wind_farm_4x3
+    from lesgo_gb300.validate import batch_vs_alone, compare, ensemble, long_run, wind_farm_4x3
+    if args.validate == "D":
+        steps = args.val_steps or 500
+        window = min(args.val_window, steps // 2)
+        r = batch_vs_alone(batch_instances(), steps=steps, window=window)
+        worst = max(max(c["u_linf"], c["uw_linf"]) for c in r["per_class"].values())
+        line = {"validate": "D", "instances": len(r["rows"]), "steps": steps, "window": window, "nskip": 10,
+                "batch": "mixed, one batch per grid class", "alone": "fp64 (plain FP64 form), one instance at a time",
+                "bar": "u_linf <= 0.01 and uw_linf <= 0.01 per instance", "pass": worst <= 0.01,
+                "per_class": r["per_class"], "wall_s": r["wall_s"], "rows": r["rows"]}
+        print(json.dumps(line), flush=True)
+        return
     if args.validate == "B":
         kw = dict(nx=128, ny=128, Nz=128)
         turbines = None

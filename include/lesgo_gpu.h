@@ -43,8 +43,11 @@ enum {
 /* ---- precision forms ---------------------------------------------------- */
 enum {
   LESGO_FP64 = 0,   /* plain FP64 drop-in                                    */
-  LESGO_MIXED = 1   /* FP32 fields and transforms; FP64 pressure RHS,
+  LESGO_MIXED = 1,  /* FP32 fields and transforms; FP64 pressure RHS,
                        tridiagonal solve, kx=ky=0 mode and wall log law      */
+  LESGO_FP64_DW = 2 /* FP64 fields and pointwise arithmetic; the x-y
+                       transforms in double-word (FP32 pair, 48-bit
+                       significand) arithmetic on the FP32 pipe              */
 };
 
 /* ---- field identifiers (sim_param.f90:300-365, sgs_param.f90:30-184) ---- */
@@ -89,7 +92,7 @@ typedef struct {
   int use_mean_p_force, eval_mean_p_force;
   double mean_p_force_x, mean_p_force_y;
   int initu;                       /* restart semantics (initial.f90:98-106) */
-  int precision;                   /* LESGO_FP64 or LESGO_MIXED              */
+  int precision;                   /* LESGO_FP64, LESGO_MIXED, LESGO_FP64_DW */
   /* actuator-disk turbines (TURBINES block); n_turbines = 0 disables */
   int n_turbines;
   const lesgo_turbine_t* turbines;

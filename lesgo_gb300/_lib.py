@@ -13,7 +13,7 @@ from .build import LIB
 
 # status codes and enums (include/lesgo_gpu.h)
 LESGO_OK, LESGO_ERR_ARG, LESGO_ERR_CUDA, LESGO_ERR_UNSUPPORTED, LESGO_ERR_NOMEM, LESGO_ERR_NUMERIC = range(6)
-LESGO_FP64, LESGO_MIXED = 0, 1
+LESGO_FP64, LESGO_MIXED, LESGO_FP64_DW = 0, 1, 2
 
 FIELD_NAMES = [
     "u", "v", "w", "dudx", "dudy", "dudz", "dvdx", "dvdy", "dvdz", "dwdx", "dwdy", "dwdz",

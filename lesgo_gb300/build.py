@@ -1,4 +1,8 @@
-"""In-tree build of the CUDA library ``liblesgo_gpu.so`` for sm_103a."""
+"""In-tree build of the CUDA library ``liblesgo_gpu.so`` for sm_103a.
+
+The solver template is instantiated once per precision form in its own
+translation unit; the units compile in parallel and link into one shared
+library."""
 from __future__ import annotations
 
 import os
@@ -7,15 +11,15 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "liblesgo_gpu.so")
-SOURCES = [os.path.join(HERE, "csrc", "solver.cu")]
-DEPS = SOURCES + sorted(os.path.join(HERE, "csrc", f) for f in os.listdir(os.path.join(HERE, "csrc"))
+OBJDIR = os.path.join(HERE, "_build")
+SOURCES = [os.path.join(CSRC, f) for f in ("solver.cu", "solver_fp32.cu", "solver_fp64.cu", "solver_dw.cu")]
+DEPS = SOURCES + sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
                         if f.endswith((".cuh", ".hpp"))) + [os.path.join(ROOT, "include", "lesgo_gpu.h")]
 
-NVCC_FLAGS = [
-    "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
-    "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-shared",
-]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:
@@ -36,12 +40,27 @@ def build(force: bool = False, verbose: bool = False) -> str:
     """Compile the library if it is missing or older than its sources."""
     if not force and up_to_date():
         return LIB
-    tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc(), *NVCC_FLAGS, "-I" + os.path.join(ROOT, "include"), *SOURCES, "-o", tmp]
+    os.makedirs(OBJDIR, exist_ok=True)
+    tag = "%d" % os.getpid()
+    objs, procs = [], []
+    for src in SOURCES:
+        obj = os.path.join(OBJDIR, os.path.basename(src).replace(".cu", ".%s.o" % tag))
+        cmd = [nvcc(), *NVCC_FLAGS, "-I" + os.path.join(ROOT, "include"), "-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((subprocess.Popen(cmd), cmd))
+        objs.append(obj)
+    failed = [cmd for p, cmd in procs if p.wait() != 0]
+    if failed:
+        raise subprocess.CalledProcessError(1, failed[0])
+    tmp = LIB + ".tmp" + tag
+    link = [nvcc(), *ARCH, "-shared", *objs, "-o", tmp]
     if verbose:
-        print(" ".join(cmd), file=sys.stderr)
-    subprocess.run(cmd, check=True)
+        print(" ".join(link), file=sys.stderr)
+    subprocess.run(link, check=True)
     os.replace(tmp, LIB)
+    for o in objs:
+        os.remove(o)
     return LIB
 
 

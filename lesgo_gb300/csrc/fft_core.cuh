@@ -22,15 +22,89 @@
 
 #include <type_traits>
 
+#include "df64.cuh"
+
 namespace lesgo {
+
+// Arithmetic types of the transforms: float (the mixed form), double (the
+// plain FP64 form) and df64 (FP64 storage with double-word transforms).
+// cplx<A> is the complex type held in shared memory and in the spectral
+// buffers.
+struct dfc {
+  df64 x, y;
+};
 
 template <typename R> struct CplxOf;
 template <> struct CplxOf<double> { using T = double2; };
 template <> struct CplxOf<float> { using T = float2; };
+template <> struct CplxOf<df64> { using T = dfc; };
 template <typename R> using cplx = typename CplxOf<R>::T;
 
 __host__ __device__ __forceinline__ double2 mkc(double a, double b) { return make_double2(a, b); }
 __host__ __device__ __forceinline__ float2 mkc(float a, float b) { return make_float2(a, b); }
+__host__ __device__ __forceinline__ dfc mkc(df64 a, df64 b) { return dfc{a, b}; }
+
+// Constants of the butterflies in each arithmetic (the double-word ones
+// split exactly: hi = the FP32 rounding, lo = the FP32 rounding of the rest).
+template <typename R> struct FftConst;
+template <> struct FftConst<float> {
+  __device__ static float sin60() { return 0.86602540378443864676f; }
+  __device__ static float rsqrt2() { return 0.70710678118654752440f; }
+  __device__ static float half() { return 0.5f; }
+  __device__ static float zero() { return 0.f; }
+  __device__ static float one() { return 1.f; }
+};
+template <> struct FftConst<double> {
+  __device__ static double sin60() { return 0.86602540378443864676372317075294; }
+  __device__ static double rsqrt2() { return 0.70710678118654752440084436210485; }
+  __device__ static double half() { return 0.5; }
+  __device__ static double zero() { return 0.0; }
+  __device__ static double one() { return 1.0; }
+};
+template <> struct FftConst<df64> {
+  __device__ static df64 sin60() { return df64{__int_as_float(0x3f5db3d7), __int_as_float(0x328584cb)}; }
+  __device__ static df64 rsqrt2() { return df64{__int_as_float(0x3f3504f3), __int_as_float(0x324fe77a)}; }
+  __device__ static df64 half() { return df64{0.5f, 0.f}; }
+  __device__ static df64 zero() { return df64{0.f, 0.f}; }
+  __device__ static df64 one() { return df64{1.f, 0.f}; }
+};
+template <typename R> __device__ __forceinline__ R rmul_half(R a) { return FftConst<R>::half() * a; }
+template <> __device__ __forceinline__ df64 rmul_half<df64>(df64 a) { return df64{0.5f * a.hi, 0.5f * a.lo}; }
+template <typename T2> __device__ __forceinline__ T2 czero() {
+  using R = decltype(T2{}.x);
+  return mkc(FftConst<R>::zero(), FftConst<R>::zero());
+}
+
+// Conversions between the storage and arithmetic types.
+template <typename D> struct Cvt;
+template <> struct Cvt<float> {
+  __device__ static float from(float a) { return a; }
+  __device__ static float from(double a) { return (float)a; }
+  __device__ static float from(df64 a) { return a.hi + a.lo; }
+};
+template <> struct Cvt<double> {
+  __device__ static double from(float a) { return (double)a; }
+  __device__ static double from(double a) { return a; }
+  __device__ static double from(df64 a) { return df_to(a); }
+};
+template <> struct Cvt<df64> {
+  __device__ static df64 from(float a) { return df64{a, 0.f}; }
+  __device__ static df64 from(double a) { return df_from(a); }
+  __device__ static df64 from(df64 a) { return a; }
+};
+template <typename D, typename S> __device__ __forceinline__ D cvt(S a) { return Cvt<D>::from(a); }
+template <typename D2, typename S2> __device__ __forceinline__ D2 cvt2(S2 a) {
+  using D = decltype(D2{}.x);
+  return mkc(cvt<D>(a.x), cvt<D>(a.y));
+}
+
+// Read-only loads of table entries.
+__device__ __forceinline__ float2 ldt(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ double2 ldt(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ dfc ldt(const dfc* p) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  return dfc{df64{v.x, v.y}, df64{v.z, v.w}};
+}
 
 template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { return mkc(a.x + b.x, a.y + b.y); }
 template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { return mkc(a.x - b.x, a.y - b.y); }
@@ -107,9 +181,9 @@ __device__ __forceinline__ void bfly4(T2& a0, T2& a1, T2& a2, T2& a3) {
 template <typename T2, bool INV>
 __device__ __forceinline__ void bfly3(T2& a0, T2& a1, T2& a2) {
   using R = decltype(a0.x);
-  const R s = (R)0.86602540378443864676372317075294;  // sin(2 pi / 3)
+  const R s = FftConst<R>::sin60();  // sin(2 pi / 3)
   T2 t1 = cadd(a1, a2);
-  T2 t2 = mkc(a0.x - (R)0.5 * t1.x, a0.y - (R)0.5 * t1.y);
+  T2 t2 = mkc(a0.x - rmul_half(t1.x), a0.y - rmul_half(t1.y));
   T2 d = csub(a1, a2);
   T2 t3 = mkc(s * d.x, s * d.y);
   a0 = cadd(a0, t1);
@@ -127,7 +201,7 @@ __device__ __forceinline__ void bfly3(T2& a0, T2& a1, T2& a2) {
 template <typename T2, bool INV>
 __device__ __forceinline__ void bfly8(T2* v) {
   using R = decltype(v[0].x);
-  const R h = (R)0.70710678118654752440084436210485;
+  const R h = FftConst<R>::rsqrt2();
   // two radix-4 on even/odd, then combine with W8 twiddles
   T2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
   T2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
@@ -149,7 +223,7 @@ __device__ __forceinline__ void bfly8(T2* v) {
 
 template <typename T2, bool INV>
 __device__ __forceinline__ T2 twid(const T2* tw, int idx, T2 a) {
-  T2 w = __ldg(tw + idx);
+  T2 w = ldt(tw + idx);
   return INV ? cmulconj(a, w) : cmul(a, w);
 }
 
@@ -198,11 +272,18 @@ __device__ __forceinline__ void lines_stage(const T2* a, T2* b, int nl, int ls, 
   }
 }
 
+// Double-word plans use radix 4, 3 and 2 only: their butterflies are long,
+// and leaving radix 8 out of them keeps the kernels' code (and its compile
+// time) small at the same arithmetic per point.
+template <typename T2> constexpr bool kRadix8 = !std::is_same<T2, dfc>::value;
+
 template <typename T2, bool INV, bool FIRST>
 __device__ __forceinline__ void lines_stage_r(int Rr, const T2* a, T2* b, int nl, int ls, int nb, int Ns,
                                               const FastDiv& fnl, const FastDiv& fns, const T2* stw) {
   switch (Rr) {
-    case 8: lines_stage<T2, INV, 8, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw); break;
+    case 8:
+      if constexpr (kRadix8<T2>) lines_stage<T2, INV, 8, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw);
+      break;
     case 4: lines_stage<T2, INV, 4, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw); break;
     case 3: lines_stage<T2, INV, 3, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw); break;
     default: lines_stage<T2, INV, 2, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw); break;
@@ -241,11 +322,13 @@ struct XfGeom {
 };
 
 // Xf: r2c along x for NF fields at once.  Src::load2(n, jy, li, v[NF])
-// supplies the real pairs (x[2n], x[2n+1]) of every field at row (jy, li).
+// supplies the real pairs (x[2n], x[2n+1]) of every field at row (jy, li)
+// in the fields' storage type (Src::C), converted to the arithmetic type R.
 // Output: out[f][li][jy][kx] for kx < K.
 template <typename R, int NF, class Src>
 __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src, cplx<R>* __restrict__ out) {
   using T2 = cplx<R>;
+  using SC = typename Src::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2* A = reinterpret_cast<T2*>(smem_raw);
   const int nl = NF * g.rpc;
@@ -256,21 +339,20 @@ __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src
   for (int t = threadIdx.x; t < g.rpc * H; t += blockDim.x) {
     const int r = g.fH.div(t), nn = t - r * H;
     const int row = row0 + r;
-    T2 v[NF];
+    SC v[NF];
     if (row < g.nrows) {
       const int li = g.fnyrows.div(row);
       const int jy = row - li * g.nyrows;
       src.load2(nn, jy, li, v);
     } else {
 #pragma unroll
-      for (int f = 0; f < NF; ++f) v[f] = mkc((R)0, (R)0);
+      for (int f = 0; f < NF; ++f) v[f] = czero<SC>();
     }
 #pragma unroll
-    for (int f = 0; f < NF; ++f) A[(f * g.rpc + r) * g.ls + nn] = v[f];
+    for (int f = 0; f < NF; ++f) A[(f * g.rpc + r) * g.ls + nn] = cvt2<T2>(v[f]);
   }
   __syncthreads();
   T2* Z = fft_lines<R, false>(A, B, nl, g.ls, g.fnl, plan);
-  const R half = (R)0.5;
   #pragma unroll 4
   for (int t = threadIdx.x; t < nl * g.K; t += blockDim.x) {
     const int l = g.fK.div(t), kk = t - l * g.K;
@@ -281,10 +363,10 @@ __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src
     T2 zm = Z[l * g.ls + (kk == 0 ? 0 : H - kk)];
     T2 a = mkc(zk.x + zm.x, zk.y - zm.y);   // Zk + conj(Zm)
     T2 b = mkc(zk.x - zm.x, zk.y + zm.y);   // Zk - conj(Zm)
-    T2 w = __ldg(plan.rtw + kk);
+    T2 w = ldt(plan.rtw + kk);
     // X = a/2 - (i/2) w b
     R wbx = w.x * b.x - w.y * b.y, wby = w.x * b.y + w.y * b.x;
-    out[(long long)f * g.out_field_stride + (long long)row * g.K + kk] = mkc(half * (a.x + wby), half * (a.y - wbx));
+    out[(long long)f * g.out_field_stride + (long long)row * g.K + kk] = mkc(rmul_half(a.x + wby), rmul_half(a.y - wbx));
   }
 }
 
@@ -300,7 +382,8 @@ struct XiGeom {
 };
 
 // Xi: c2r along x for NF fields at once, then Dst::store(jy, li, i, vals)
-// receives the NF reconstructed reals at x index i of row (jy, li).
+// receives the NF reconstructed reals at x index i of row (jy, li), in the
+// fields' storage type (Dst::Real).
 template <typename R, int NF, class Dst>
 __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const cplx<R>* __restrict__ in, Dst dst) {
   using T2 = cplx<R>;
@@ -316,15 +399,15 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
     const int l = g.fH.div(t), k = t - l * H;
     const int f = g.frpc.div(l), r = l - f * g.rpc;
     const int row = row0 + r;
-    T2 z = mkc((R)0, (R)0);
+    T2 z = czero<T2>();
     if (row < g.nrows) {
       const T2* src = in + (long long)f * g.in_field_stride + (long long)row * g.K;
-      T2 xk = k < g.K ? src[k] : mkc((R)0, (R)0);
+      T2 xk = k < g.K ? src[k] : czero<T2>();
       const int km = H - k;   // k = 0 -> Nyquist (zero)
-      T2 xm = (k > 0 && km < g.K) ? src[km] : mkc((R)0, (R)0);
+      T2 xm = (k > 0 && km < g.K) ? src[km] : czero<T2>();
       T2 a = mkc(xk.x + xm.x, xk.y - xm.y);
       T2 b = mkc(xk.x - xm.x, xk.y + xm.y);
-      T2 w = __ldg(plan.rtw + k);
+      T2 w = ldt(plan.rtw + k);
       R cx = w.x * b.x + w.y * b.y, cy = w.x * b.y - w.y * b.x;  // conj(w) * b
       z = mkc(a.x - cy, a.y + cx);
     }
@@ -340,9 +423,9 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
     if (row >= g.nrows) continue;
     const int li = g.fnyrows.div(row);
     const int jy = row - li * g.nyrows;
-    R vals[NF];
+    typename Dst::Real vals[NF];
 #pragma unroll
-    for (int f = 0; f < NF; ++f) vals[f] = Zr[2 * ((f * g.rpc + r) * g.ls) + i];
+    for (int f = 0; f < NF; ++f) vals[f] = cvt<typename Dst::Real>(Zr[2 * ((f * g.rpc + r) * g.ls) + i]);
     dst.store(jy, li, i, vals);
   }
 }
@@ -380,7 +463,9 @@ template <typename T2, bool INV, bool FIRST>
 __device__ __forceinline__ void cols_stage_r(int Rr, const T2* a, T2* b, int width, const FastDiv& fw, int nb, int Ns,
                                              const FastDiv& fns, const T2* stw) {
   switch (Rr) {
-    case 8: cols_stage<T2, INV, 8, FIRST>(a, b, width, fw, nb, Ns, fns, stw); break;
+    case 8:
+      if constexpr (kRadix8<T2>) cols_stage<T2, INV, 8, FIRST>(a, b, width, fw, nb, Ns, fns, stw);
+      break;
     case 4: cols_stage<T2, INV, 4, FIRST>(a, b, width, fw, nb, Ns, fns, stw); break;
     case 3: cols_stage<T2, INV, 3, FIRST>(a, b, width, fw, nb, Ns, fns, stw); break;
     default: cols_stage<T2, INV, 2, FIRST>(a, b, width, fw, nb, Ns, fns, stw); break;
@@ -433,38 +518,34 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
   const int rstep = blockDim.x >> g.tk_log2;
   const bool live = c < tkv;
   const int kx = kx0 + c;
+  // the forward transform's stages alternate between the tile and the
+  // scratch: load into the buffer from which they end in S
+  T2* L = (FWD && (pin.nf & 1)) ? X : S;
 #pragma unroll
   for (int i = 0; i < NIN; ++i) {
     const auto* src = op.in_plane(grp, i, li) + kx;
-    T2* s = S + i * g.tk + c;
+    T2* s = L + i * g.tk + c;
 #pragma unroll 4
     for (int jy = r0; jy < g.ny_in; jy += rstep) {
-      T2 v = mkc((R)0, (R)0);
-      if (live) {
-        const auto a = src[(long long)jy * g.K];
-        v = mkc((R)a.x, (R)a.y);
-      }
+      T2 v = czero<T2>();
+      if (live) v = cvt2<T2>(src[(long long)jy * g.K]);
       s[jy * win] = v;
     }
   }
   __syncthreads();
-  if (FWD) {
-    T2* res = fft_cols<R, false>(S, X, win, g.fwin, pin);
-    if (res != S) {
-      for (int t = threadIdx.x; t < win * g.ny_in; t += blockDim.x) S[t] = res[t];
-      __syncthreads();
-    }
-  }
+  if (FWD) fft_cols<R, false>(L, L == S ? X : S, win, g.fwin, pin);   // ends in S
   for (int o = 0; o < NOUT; ++o) {
 #pragma unroll 2
     for (int ky = r0; ky < g.ny_out; ky += rstep) {
-      T2 acc = mkc((R)0, (R)0);
+      T2 acc = czero<T2>();
       const int kin = op.rowmap(ky);
       if (live && kin >= 0) {
 #pragma unroll
         for (int i = 0; i < NIN; ++i) {
           T2 cf;
-          if (op.coef(grp, o, i, kx, kin, cf)) acc = cadd(acc, cmul(S[kin * win + i * g.tk + c], cf));
+          const T2 v = S[kin * win + i * g.tk + c];
+          if (op.is_one(o, i)) acc = cadd(acc, v);
+          else if (op.coef(grp, o, i, kx, kin, cf)) acc = cadd(acc, cmul(v, cf));
         }
       }
       W0[ky * g.tk + c] = acc;
@@ -477,10 +558,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
       using OutT = typename std::remove_pointer<decltype(dst)>::type;
 #pragma unroll 4
       for (int ky = r0; ky < g.ny_out; ky += rstep) {
-        const T2 v = res[ky * g.tk + c];
-        OutT w;
-        w.x = v.x; w.y = v.y;
-        dst[(long long)ky * g.K] = w;
+        dst[(long long)ky * g.K] = cvt2<OutT>(res[ky * g.tk + c]);
       }
     }
     __syncthreads();

@@ -1069,7 +1069,7 @@ __global__ void __launch_bounds__(256) k_diag(const R* dudx, const R* dvdy, cons
   if (threadIdx.x < 7) partial[blockIdx.x * 7 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-__global__ void k_diag_final(const double* partial, int nblocks, double* out) {
+static __global__ void k_diag_final(const double* partial, int nblocks, double* out) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int b = 0; b < nblocks; ++b)
@@ -1084,7 +1084,7 @@ __global__ void k_diag_final(const double* partial, int nblocks, double* out) {
 // host-side formulas of lesgo_gpu_diag applied on the device (rmsdiv.f90,
 // io.f90:99-141, cfl_util.f90:35-64, functions.f90:882-905): jt_total,
 // total_time, rmsdiv, ke, cfl, tau_wall_bot.
-__global__ void k_diag_log_final(const double* partial, int nblocks, const double* sc_row, double* row,
+static __global__ void k_diag_log_final(const double* partial, int nblocks, const double* sc_row, double* row,
                                  double jt_total, double npts, double nxy, double dx, double dy, double dz) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -1236,7 +1236,7 @@ __device__ __forceinline__ double sched_interp(const double* x, const double* v,
 }
 
 // One thread per turbine.
-__global__ void k_turb_controls(TurbDyn a) {
+static __global__ void k_turb_controls(TurbDyn a) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.nturb) return;
   const int n = a.nturb;
@@ -1288,7 +1288,7 @@ __device__ __forceinline__ double turb_ind_val(const double* r, const double* R2
 // and normalise them to integrate to one (turbines.f90:388-437).  The
 // geometry is rounded operation by operation as the reference evaluates it
 // (no fused multiply-adds: r*r - r_norm*r_norm is exactly zero on the axis).
-__global__ void __launch_bounds__(256) k_turb_nodes(TurbDyn a) {
+static __global__ void __launch_bounds__(256) k_turb_nodes(TurbDyn a) {
   __shared__ double sh[256];
   const int s = a.dyn_list[blockIdx.x];
   const double n0 = a.nhat[3 * s], n1 = a.nhat[3 * s + 1], n2 = a.nhat[3 * s + 2];
@@ -1368,7 +1368,7 @@ namespace lesgo {
 // thread per (kx, ky) column: u(1) = r(1)/b(1) for every kx < nx/2, then
 // the Thomas sweeps skip the ky Nyquist row and the kx = ky = 0 column.
 // `gam` is scratch of lh*ny*n doubles; a zero pivot sets *err.
-__global__ void __launch_bounds__(128) k_tridag(const double* __restrict__ a, const double* __restrict__ b,
+static __global__ void __launch_bounds__(128) k_tridag(const double* __restrict__ a, const double* __restrict__ b,
                                                 const double* __restrict__ c, const double2* __restrict__ r,
                                                 double2* __restrict__ u, double* __restrict__ gam,
                                                 int lh, int ny, int n, int* err) {
@@ -1467,7 +1467,7 @@ __global__ void k_tavg(TavgArgs<R> a) {
 // The time average of quantity `which` (accumulator / total time), or a
 // Reynolds stress (time_average.f90:616-629): 26 u'u', 27 v'v', 28 w'w',
 // 29 u'v', 30 u'w' (w grid), 31 v'w' (w grid).  One instance, levels 0..nz.
-__global__ void k_tavg_get(const double* acc, long long acc_stride, long long ib, int which, double inv_t,
+static __global__ void k_tavg_get(const double* acc, long long acc_stride, long long ib, int which, double inv_t,
                            double* out, long long n) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
@@ -1486,7 +1486,7 @@ __global__ void k_tavg_get(const double* acc, long long acc_stride, long long ib
 }
 
 // Plane mean over x < nx of a (ld, ny, levels) double array: one block per level.
-__global__ void k_plane_mean(const double* f, int nx, int ny, int ld, double* out) {
+static __global__ void k_plane_mean(const double* f, int nx, int ny, int ld, double* out) {
   __shared__ double sh[256];
   const long long base = (long long)blockIdx.x * ny * ld;
   double s = 0.0;
@@ -1556,7 +1556,7 @@ struct StepBeginArgs {
   double cfl, dx, dy, dz, c1, z_i, u_star, T_avg_dim;
 };
 
-__global__ void k_step_begin(StepBeginArgs a) {
+static __global__ void k_step_begin(StepBeginArgs a) {
   const int inst = blockIdx.x * blockDim.x + threadIdx.x;
   if (inst >= a.ninst) return;
   double* c = a.sc + inst * SC_N;
@@ -1592,7 +1592,7 @@ __global__ void k_step_begin(StepBeginArgs a) {
 // starts fresh sums (tavg%init), 2 starts from sums read from tavg.out, 3
 // takes a sample weighted by the pending time (tavg%compute); w receives the
 // sample weight (0: none).
-__global__ void k_tavg_prep(double* sc, const int* act, double* w, int ninst) {
+static __global__ void k_tavg_prep(double* sc, const int* act, double* w, int ninst) {
   const int inst = blockIdx.x * blockDim.x + threadIdx.x;
   if (inst >= ninst) return;
   double* c = sc + inst * SC_N;

@@ -65,6 +65,7 @@ struct InstMap {
 // With `isc` set, the scale is the instance's step constant isc[inst][isc_idx].
 template <typename R, int NF>
 struct SrcFields {
+  using C = cplx<R>;   // the fields' complex pair type
   const R* p[NF];
   R scale;
   int lev0, levstride, ld;
@@ -90,6 +91,7 @@ struct SrcFields {
 // velocity spectra from filt_da's forward pass).
 template <typename R, bool VORT_ONLY = false>
 struct SrcVort {
+  using C = cplx<R>;   // the fields' complex pair type
   const R *u, *v, *w, *dudy, *dudz, *dvdx, *dvdz, *dwdx, *dwdy;
   R c;
   int ld, nz, lbc, ubc;
@@ -140,6 +142,7 @@ struct SrcVort {
 // the normalisation 1/(nx2*ny2), levels 1..nz.
 template <typename R>
 struct SrcConvProd {
+  using C = cplx<R>;   // the fields' complex pair type
   const R *ub, *vb, *wb, *o1, *o2, *o3;
   R c;
   int ld, nz;
@@ -179,6 +182,7 @@ struct SrcConvProd {
 // levels 1..nz (w-nodes; uv-node at the wall).
 template <typename R>
 struct SrcLagrange {
+  using C = cplx<R>;   // the fields' complex pair type
   const R *u, *v, *w, *S11, *S12, *S13, *S22, *S23, *S33;
   int ld, nz, lbc, ubc;
   long long plane;
@@ -222,6 +226,7 @@ struct SrcLagrange {
 enum : int { MUL_ZERO = 0, MUL_ONE = 1, MUL_IKX = 2, MUL_IKY = 3, MUL_G1 = 4, MUL_G2 = 5 };
 enum : int { ROW_SAME = 0, ROW_PAD = 1, ROW_UNPAD = 2 };
 
+// R is the transforms' arithmetic type (the multiplier tables are held in it).
 template <typename R, int NIN, int NOUT, typename InT, typename OutT>
 struct YOpLin {
   const InT* in;
@@ -258,13 +263,15 @@ struct YOpLin {
     if (ko == hs) return -1;
     return ko + ny_big - ny_small;
   }
+  // a plain copy of input i into output o (no multiply)
+  __device__ __forceinline__ bool is_one(int o, int i) const { return mul[o][i] == MUL_ONE; }
   __device__ __forceinline__ bool coef(int g, int o, int i, int kx, int kin, cplx<R>& cf) const {
     switch (mul[o][i]) {
-      case MUL_ONE: cf = mkc((R)1, (R)0); return true;
-      case MUL_IKX: cf = mkc((R)0, kxw[kx]); return true;
-      case MUL_IKY: cf = mkc((R)0, kyw[kin]); return true;
-      case MUL_G1: cf = mkc(G1[kin * lh + kx], (R)0); return true;
-      case MUL_G2: cf = mkc(G2[kin * lh + kx], (R)0); return true;
+      case MUL_ONE: cf = mkc(FftConst<R>::one(), FftConst<R>::zero()); return true;
+      case MUL_IKX: cf = mkc(FftConst<R>::zero(), kxw[kx]); return true;
+      case MUL_IKY: cf = mkc(FftConst<R>::zero(), kyw[kin]); return true;
+      case MUL_G1: cf = mkc(G1[kin * lh + kx], FftConst<R>::zero()); return true;
+      case MUL_G2: cf = mkc(G2[kin * lh + kx], FftConst<R>::zero()); return true;
       default: return false;
     }
   }
@@ -275,6 +282,7 @@ struct YOpLin {
 // ---------------------------------------------------------------------------
 template <typename R, int NF>
 struct DstFields {
+  using Real = R;     // the fields' storage type
   R* p[NF];
   int lev0, levstride, ld;
   long long plane;
@@ -292,6 +300,7 @@ struct DstFields {
 // WHICH: 1 = divtx, divty (NF=2); 2 = divtz (NF=1); 3 = all (NF=3).
 template <typename R, int WHICH>
 struct DstDiv {
+  using Real = R;     // the fields' storage type
   R *divtx, *divty, *divtz;
   const R *txz, *tyz, *tzz;
   R inv_dz;
@@ -323,6 +332,7 @@ struct DstDiv {
 // (+ mean_p_force) (+ f_a), Euler first step, AB2 intermediate velocity.
 template <typename R, bool FUSED>
 struct DstConvec {
+  using Real = R;     // the fields' storage type
   R *RHSx, *RHSy, *RHSz, *RHSxf, *RHSyf, *RHSzf, *u, *v, *w;
   const R *divtx, *divty, *divtz, *fxa, *fya, *fza;
   const double* sc;   // step constants
@@ -378,6 +388,7 @@ struct DstConvec {
 // projection of u and v.
 template <typename R, bool FUSED>
 struct DstPress {
+  using Real = R;     // the fields' storage type
   R *p, *dpdx, *dpdy, *RHSx, *RHSy, *u, *v;
   const double* sc;   // step constants
   int ld;
@@ -409,6 +420,7 @@ struct DstPress {
 // vals[2q+1] = at 4 Delta (q as in SrcLagrange).
 template <typename R>
 struct DstLagrange {
+  using Real = R;     // the fields' storage type
   const R *FLMi, *FMMi, *FQNi, *FNNi;  // interpolated running averages
   R *FLM, *FMM, *FQN, *FNN, *Cs, *Beta, *Tn_all, *ee_now;
   double cst, opftdelta, beta_exp;

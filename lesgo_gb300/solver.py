@@ -35,6 +35,10 @@ class LesgoError(RuntimeError):
         self.code = code
 
 
+# precision forms: FP64 throughout; FP32 bulk with the FP64 pressure solve;
+# FP64 fields with double-word (FP32 pair) x-y transforms
+PRECISIONS = {"fp64": L.LESGO_FP64, "mixed": L.LESGO_MIXED, "fp64dw": L.LESGO_FP64_DW}
+
 PARAM_DEFAULTS = dict(
     nx=64, ny=64, Nz=64, L_x=2.0 * 3.1415926535897932384626433, L_y=3.1415926535897932384626433, L_z=1.0,
     z_i=1000.0, u_star=0.45, vonk=0.4, zo=1.0e-4, dt=2.0e-4, sgs_model=5, cs_count=5, dyn_init=100,
@@ -61,7 +65,7 @@ def make_params(**kw) -> L.Params:
     for name in ("molec", "use_mean_p_force", "eval_mean_p_force", "initu", "adm_correction", "use_cfl_dt"):
         setattr(p, name, 1 if cfg[name] else 0)
     prec = cfg["precision"]
-    p.precision = {"fp64": L.LESGO_FP64, "mixed": L.LESGO_MIXED}[prec] if isinstance(prec, str) else int(prec)
+    p.precision = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
     return p, cfg
 
 

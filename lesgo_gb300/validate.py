@@ -110,3 +110,63 @@ def wind_farm_4x3(L_z: float = 1.0):
             ts.append(dict(xloc=1.0 + 7 * D * i, yloc=1.0 + 5 * D * (j - 1) + 0.5, height=0.1 * L_z, dia=D,
                            thk=0.0, theta1=0.0, theta2=0.0, Ct_prime=1.33))
     return ts
+
+
+def batch_vs_alone(instances, steps: int = 500, window: int = 250, nskip: int = 10,
+                   batch_precision: str = "mixed", alone_precision: str = "fp64", base: Optional[dict] = None):
+    """Each instance of a batched ensemble against the same instance run
+    alone.  `instances` is a list of ((nx, ny, Nz), zo, seed).  The batch
+    runs one handle per grid class in `batch_precision`; every instance then
+    runs alone in `alone_precision` from the same seeded IC.  Per instance:
+    the time-averaged <u>(z) and resolved <u'w'>(z) over the last `window`
+    steps (sampled every `nskip`) and the plane-mean u(z) after the last
+    step, each as max_z |batch - alone| / max_z |alone|.  Returns the rows
+    and their worst value per grid class."""
+    from .solver import LesgoBatch
+    base = dict(base or dict(dyn_init=5, cs_count=5))
+    first = steps - window if steps > window else nskip
+    by_grid: Dict[tuple, list] = {}
+    for g, zo, seed in instances:
+        by_grid.setdefault(tuple(g), []).append((zo, seed))
+    rows = []
+    t_batch = t_alone = 0.0
+    for g, lst in by_grid.items():
+        kw = dict(nx=g[0], ny=g[1], Nz=g[2], **base)
+        nz = g[2] + 1
+        b = LesgoBatch(len(lst), precision=batch_precision, **kw)
+        try:
+            ids = [b.add(zo, seed) for zo, seed in lst]
+            b.tavg_config(first, steps, nskip)
+            t0 = time.perf_counter()
+            b.step(steps)
+            b.sync()
+            t_batch += time.perf_counter() - t0
+            res_b = {iid: dict(u=b.tavg_profile(iid, "u"), upwp=b.tavg_profile(iid, "upwp"),
+                               um=b.get(iid, "u")[1:nz, :, :g[0]].mean(axis=(1, 2))) for iid in ids}
+        finally:
+            b.close()
+        for (zo, seed), iid in zip(lst, ids):
+            a = LesgoGPU(zo=zo, precision=alone_precision, **kw)
+            try:
+                a.init_ic(seed)
+                a.tavg_config(first, steps, nskip)
+                t0 = time.perf_counter()
+                a.step(steps)
+                a.sync()
+                t_alone += time.perf_counter() - t0
+                ua, wa = a.tavg_profile("u")[1:nz], a.tavg_profile("upwp")[1:nz + 1]
+                uma = a.get("u")[1:nz, :, :g[0]].mean(axis=(1, 2))
+            finally:
+                a.close()
+            rb = res_b[iid]
+            rows.append(dict(grid="x".join(map(str, g)), zo=zo, seed=seed,
+                             u_linf=float(np.max(np.abs(rb["u"][1:nz] - ua)) / np.max(np.abs(ua))),
+                             uw_linf=float(np.max(np.abs(rb["upwp"][1:nz + 1] - wa)) / np.max(np.abs(wa))),
+                             plane_u_linf=float(np.max(np.abs(rb["um"] - uma)) / np.max(np.abs(uma)))))
+    per_class = {}
+    for r in rows:
+        c = per_class.setdefault(r["grid"], dict(instances=0, u_linf=0.0, uw_linf=0.0, plane_u_linf=0.0))
+        c["instances"] += 1
+        for k in ("u_linf", "uw_linf", "plane_u_linf"):
+            c[k] = max(c[k], r[k])
+    return dict(rows=rows, per_class=per_class, wall_s=dict(batch=t_batch, alone=t_alone))

@@ -29,21 +29,33 @@ def _threads(o):
 
 
 def test_halfchannel_128_10_steps_fp64(built_lib):
+    """Both FP64-field forms (FP64 transforms; double-word transforms)
+    against one oracle run."""
+    from lesgo_gb300.solver import LesgoGPU
     p, o, g = make_pair(nx=128, ny=128, Nz=128, dyn_init=5, cs_count=5)
+    g2 = LesgoGPU(nx=128, ny=128, Nz=128, dyn_init=5, cs_count=5, precision="fp64dw")
+    g2.init_ic(1)
     _threads(o)
     for _ in range(10):
         o.step()
-    g.step(10)
-    g.sync()
-    errs = {f: rel_err(p, f, g.get(f), oracle_field(o, f)) for f in FIELDS}
-    d = g.diag()
-    print("\n128^3 fp64 after 10 steps:", " ".join(f"{f}={e:.2e}" for f, e in errs.items()),
-          f"rmsdiv gpu={d['rmsdiv']:.6e} oracle={o.rmsdiv():.6e}")
-    for f, e in errs.items():
-        assert e < STEP_TOL, (f, e)
-    assert abs(d["rmsdiv"] - o.rmsdiv()) < 1e-12 + 1e-6 * o.rmsdiv()
-    assert abs(d["ke"] - o.energy()) / o.energy() < 1e-12
-    g.close()
+    for form, gg in (("fp64", g), ("fp64dw", g2)):
+        gg.step(10)
+        gg.sync()
+        errs = {f: rel_err(p, f, gg.get(f), oracle_field(o, f)) for f in FIELDS}
+        d = gg.diag()
+        print(f"\n128^3 {form} after 10 steps:", " ".join(f"{f}={e:.2e}" for f, e in errs.items()),
+              f"rmsdiv gpu={d['rmsdiv']:.6e} oracle={o.rmsdiv():.6e}")
+        for f, e in errs.items():
+            assert e < STEP_TOL, (form, f, e)
+        if form == "fp64":
+            assert abs(d["rmsdiv"] - o.rmsdiv()) < 1e-12 + 1e-6 * o.rmsdiv()
+        else:
+            # the divergence left by the projection is round-off of the
+            # transforms' 48-bit significand: 6e-12 at 128^3 against a
+            # velocity-gradient scale of u/dz ~ 3e3, i.e. 2e-15 relative
+            assert d["rmsdiv"] < 1e-10
+        assert abs(d["ke"] - o.energy()) / o.energy() < 1e-12
+        gg.close()
 
 
 @pytest.mark.parametrize("dyn_init,seed", [(100, 1)] + [(5, s) for s in range(1, 6)])

@@ -37,11 +37,12 @@ def test_ic_matches_oracle(built_lib):
         assert e < 1e-15, (name, e)
 
 
-@pytest.mark.parametrize("dyn_init", [5, 100])
-def test_stagewise_parity_fp64(built_lib, dyn_init):
+@pytest.mark.parametrize("dyn_init,precision", [(5, "fp64"), (100, "fp64"), (5, "fp64dw")])
+def test_stagewise_parity_fp64(built_lib, dyn_init, precision):
     """Each drop-in entry point against the oracle stage it replaces, over 10
-    steps (dyn_init=5 exercises the Lagrangian update at steps 5 and 10)."""
-    p, o, g = make_pair(nx=32, ny=32, Nz=32, dyn_init=dyn_init)
+    steps (dyn_init=5 exercises the Lagrangian update at steps 5 and 10).
+    fp64dw: FP64 fields with the x-y transforms in double-word arithmetic."""
+    p, o, g = make_pair(precision, nx=32, ny=32, Nz=32, dyn_init=dyn_init)
     worst = {}
     for step in range(10):
         for name, fn, outs in o.stages():
@@ -58,10 +59,10 @@ def test_stagewise_parity_fp64(built_lib, dyn_init):
     assert max(worst.values()) < 1e-10
 
 
-@pytest.mark.parametrize("dyn_init", [5, 100])
-def test_fused_10_steps_fp64(built_lib, dyn_init):
+@pytest.mark.parametrize("dyn_init,precision", [(5, "fp64"), (100, "fp64"), (5, "fp64dw"), (100, "fp64dw")])
+def test_fused_10_steps_fp64(built_lib, dyn_init, precision):
     """The fused, graph-replayed step against the oracle after 10 steps."""
-    p, o, g = make_pair(nx=32, ny=32, Nz=32, dyn_init=dyn_init)
+    p, o, g = make_pair(precision, nx=32, ny=32, Nz=32, dyn_init=dyn_init)
     for _ in range(10):
         o.step()
     g.step(10)
@@ -86,9 +87,10 @@ def test_fused_matches_dropin_sequence(built_lib):
         assert e < 1e-11, (f, e)
 
 
-def test_uneven_grid_fp64(built_lib):
+@pytest.mark.parametrize("precision", ["fp64", "fp64dw"])
+def test_uneven_grid_fp64(built_lib, precision):
     """Non-square grid with radix-3 lengths (48 x 96 x 24, padded 72 x 144)."""
-    p, o, g = make_pair(nx=48, ny=96, Nz=24, dyn_init=5, L_y=2.0)
+    p, o, g = make_pair(precision, nx=48, ny=96, Nz=24, dyn_init=5, L_y=2.0)
     for _ in range(5):
         o.step()
     g.step(5)
