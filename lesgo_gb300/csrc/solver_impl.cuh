@@ -7,6 +7,7 @@
 #pragma once
 #include "lesgo_gpu.h"
 #include "kernels.cuh"
+#include "convec_rows.cuh"
 #include "restart_io.hpp"
 #include "conf.hpp"
 
@@ -187,6 +188,18 @@ class SolverBase {
   virtual int diag_log_read(int id, double* out, int maxrows) = 0;
 };
 
+// Whether the convective term's 3/2-grid x-rows run as one pass
+// (k_convec_rows: c2r, products and r2c in shared memory) or as three
+// (xinv to six 3/2-grid fields in HBM, products, xfwd).  One pass for the
+// mixed form, three for the FP64-field forms, whose 16-byte complex values
+// leave the one-pass kernel too few rows per block (measured slower there);
+// LESGO_CONVEC_ROWS=1 / 0 chooses for every form.
+static bool convec_rows_enabled(int precision) {
+  const char* e = std::getenv("LESGO_CONVEC_ROWS");
+  if (e) return std::strcmp(e, "0") != 0;
+  return precision == LESGO_MIXED;
+}
+
 // Device bytes of a handle (the admission footprint of a batch).
 static long long footprint_bytes(const Derived& d, int cap) {
   const long long rs = d.p.precision == LESGO_MIXED ? 4 : 8;
@@ -195,7 +208,8 @@ static long long footprint_bytes(const Derived& d, int cap) {
   const long long vs = (long long)d.nz * d.ny * d.K, vb = (long long)d.nz * d.ny2 * d.K, ps = (long long)d.ny * d.K;
   long long b = 0;
   b += (LESGO_NFIELDS + 4 + (d.turbines.empty() ? 0 : 1)) * nf * rs;   // fields, interpolation temps, fza on uv
-  b += 4 * plane * rs + 6 * (long long)(d.nz + 1) * pbig * rs;          // wall planes, 3/2-grid fields
+  b += 4 * plane * rs;                                                  // wall planes
+  if (!convec_rows_enabled(d.p.precision)) b += 6 * (long long)(d.nz + 1) * pbig * rs;   // 3/2-grid fields
   b += (std::max({21 * vs, 6 * vs, 3 * vb}) + std::max({42 * vs, 6 * vb, 9 * vs}) + 4 * ps) * 2 * rs;   // spectra
   b += (std::max(6 * vs, 3 * vb) + std::max(6 * vb, 3 * vs)) * 2 * rs;                             // convec spectra
   b += (3 * vs + 2 * ps + (long long)(d.nz + 1) * ps) * 16;                                          // FP64 pressure
@@ -249,7 +263,9 @@ class Solver : public SolverBase {
     for (int f = 0; f < LESGO_NFIELDS; ++f) F_[f] = alloc<R>(nfield_);
     for (int f = 0; f < 4; ++f) Ftmp_[f] = alloc<R>(nfield_);
     for (int f = 0; f < 4; ++f) wall_[f] = alloc<R>(kp_.plane * cap_);
-    for (int f = 0; f < 6; ++f) big_[f] = alloc<R>(kp_.istride_big * cap_);
+    conv_rows_ = convec_rows_enabled(d_.p.precision);
+    if (!conv_rows_)
+      for (int f = 0; f < 6; ++f) big_[f] = alloc<R>(kp_.istride_big * cap_);
     vol1_s_ = (long long)nz * ny * d_.K;
     vol1_b_ = (long long)nz * d_.ny2 * d_.K;
     const long long pl_s = (long long)ny * d_.K;
@@ -266,7 +282,7 @@ class Solver : public SolverBase {
     hplane_ = alloc<double2>(2 * pl_s * cap_);
     phat_ = alloc<double2>((nz + 1) * pl_s * cap_);
     build_thomas_pivots();
-    err_ = alloc<int>(1);
+    err_ = alloc<int>(2);   // [0] zero pivot, [1] a bulk-copy wait that gave up
     zo_d_ = alloc<double>(cap_);
     flags_d_ = alloc<int>(cap_);
     // pinned staging ring for the per-step uploads (flags, averaging actions):
@@ -861,9 +877,13 @@ class Solver : public SolverBase {
 
   int sync() override {
     CK(cudaStreamSynchronize(st_));
-    int e = 0;
-    CK(cudaMemcpy(&e, err_, sizeof(int), cudaMemcpyDeviceToHost));
-    if (e) {
+    int e[2] = {0, 0};
+    CK(cudaMemcpy(e, err_, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    if (e[1]) {
+      CK(cudaMemset(err_ + 1, 0, sizeof(int)));
+      throw Error(LESGO_ERR_CUDA, "a bulk copy into shared memory did not complete within its wait limit");
+    }
+    if (e[0]) {
       CK(cudaMemset(err_, 0, sizeof(int)));
       return LESGO_ERR_NUMERIC;
     }
@@ -981,7 +1001,9 @@ class Solver : public SolverBase {
         SrcFields<R, 6> src{{F_[LESGO_U], F_[LESGO_V], F_[LESGO_W], F_[LESGO_DUDX], F_[LESGO_DUDY], F_[LESGO_DUDZ]},
                             sc, 1, 1, d_.ld, kp_.plane, im};
         xfwd<6>(src, d_.nx, ny, nz, specA_, px_, "tune.xfwd");
-        DstFields<R, 6> dst{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld, kp_.plane, im};
+        // into scratch only: the interpolation temporaries (free between
+        // steps), two of them twice, which is the same work per launch
+        DstFields<R, 6> dst{{Ftmp_[0], Ftmp_[1], Ftmp_[2], Ftmp_[3], Ftmp_[0], Ftmp_[1]}, 1, 1, d_.ld, kp_.plane, im};
         xinv<6>(dst, specA_, d_.nx, ny, nz, px_, "tune.xinv");
       });
       if (ms < best) { best = ms; best_x = xt; }
@@ -1862,13 +1884,52 @@ class Solver : public SolverBase {
     }
     ypass_lin<1, 1, true, true, T2, T2>(cvA_, 0, 1, d_.nz, d_.ny, cvB_, d_.ny2, d_.nz, 6, ROW_PAD, {{MUL_ONE}},
                                         "convec.ypass_pad");
-    DstFields<R, 6> db{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld_big, kp_.plane_big, imb};
-    xinv<6>(db, cvB_, d_.nx2, d_.ny2, d_.nz, pxb_, "convec.xinv_big");
-    const R cb = (R)(1.0 / ((double)d_.nx2 * d_.ny2));
-    SrcConvProd<R> sp{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5], cb, d_.ld_big, d_.nz, kp_.plane_big, imb};
-    xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, cvA_, pxb_, "convec.xfwd_big", 6);
+    if (conv_rows_) {
+      convec_rows(HostCvt<A>::from(1.0L / ((long double)d_.nx2 * d_.ny2)));
+    } else {
+      DstFields<R, 6> db{{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5]}, 1, 1, d_.ld_big, kp_.plane_big, imb};
+      xinv<6>(db, cvB_, d_.nx2, d_.ny2, d_.nz, pxb_, "convec.xinv_big");
+      const R cb = (R)(1.0 / ((double)d_.nx2 * d_.ny2));
+      SrcConvProd<R> sp{big_[0], big_[1], big_[2], big_[3], big_[4], big_[5], cb, d_.ld_big, d_.nz, kp_.plane_big,
+                        imb};
+      xfwd<3>(sp, d_.nx2, d_.ny2, d_.nz, cvA_, pxb_, "convec.xfwd_big", 6);
+    }
     ypass_lin<1, 1, true, true, T2, T2>(cvA_, 0, 1, d_.nz, d_.ny2, cvB_, d_.ny, d_.nz, 3, ROW_UNPAD, {{MUL_ONE}},
                                         "convec.ypass_unpad");
+  }
+  // The 3/2-grid x-rows of the convective term in one pass: the six padded
+  // spectra of cvB_ in, the three products' x-spectra (nx/2 modes) into cvA_.
+  void convec_rows(A cb) {
+    ConvRowsGeom g;
+    g.M = d_.nx2; g.K = d_.K; g.ny2 = d_.ny2; g.nz = d_.nz; g.ls = d_.nx2 / 2 + 1;
+    g.in_fs = vol1_b_ * kp_.ninst;
+    g.out_fs = vol1_b_ * kp_.ninst;
+    const int H = d_.nx2 / 2;
+    // rows per block as for the other x passes, within a shared-memory
+    // budget of four blocks per SM (two for 16-byte complex values); two
+    // complex elements more hold the copy barriers
+    int rt = std::max(1, std::min(16, xtarget_ / (6 * H)));
+    auto smem_of = [&](int r) { return (size_t)(conv_rows_smem_elems(r, g.ls, d_.K) + 2) * sizeof(T2); };
+    const size_t budget = (sizeof(T2) == 16 ? 112 : 56) * 1024;
+    while (rt > 1 && smem_of(rt) > budget) --rt;
+    g.rt = rt;
+    // a chunk of at least 16 levels (each chunk repeats part of the c2r of
+    // two levels), longer chunks when the grid already fills the GPU
+    const long long tiles = (long long)((d_.ny2 + rt - 1) / rt) * kp_.ninst;
+    int cz = 16;
+    while (cz < d_.nz && tiles * ((d_.nz + cz - 1) / cz) > 8LL * 152) cz *= 2;
+    g.cz = std::min(cz, d_.nz);
+    g.fH = FastDiv((unsigned)H); g.fK = FastDiv((unsigned)d_.K);
+    g.f2 = FastDiv((unsigned)(2 * rt)); g.f3 = FastDiv((unsigned)(3 * rt)); g.f6 = FastDiv((unsigned)(6 * rt));
+    g.frt = FastDiv((unsigned)rt);
+    g.err = err_ + 1;
+    const size_t smem = smem_of(rt);
+    auto kern = k_convec_rows<A>;
+    set_smem(kern, smem);
+    dim3 grid((unsigned)((d_.ny2 + rt - 1) / rt), (unsigned)((d_.nz + g.cz - 1) / g.cz), (unsigned)kp_.ninst);
+    pre();
+    kern<<<grid, 256, smem, st_>>>(g, pxb_, cvB_, cvA_, cb);
+    post("convec.rows", 9.0 * vol1_b_ * kp_.ninst * sizeof(T2));
   }
   void convec_part2(bool fused) {
     const InstMap im = imf(d_.nz);
@@ -2088,6 +2149,7 @@ class Solver : public SolverBase {
   int launches_ = 0;
   bool prof_on_ = false;
   bool branches_allowed_ = true;   // LESGO_BRANCHES=0: the fused step on one stream
+  bool conv_rows_ = false;         // the one-pass 3/2-grid x-rows of the convective term
   cudaEvent_t prof_start_ = nullptr;
   std::vector<ProfRec> prof_;
   std::map<int, cudaGraphExec_t> graphs_;

@@ -267,3 +267,41 @@ def test_mixed_lagrangian_boundary_cases(built_lib, case):
         bar = MIXED_TOL if f in ("u", "w") else (1e-2 if f == "Cs_opt2" else 5 * MIXED_TOL)
         assert e < bar, (case, f, e)
     g.close()
+
+
+@pytest.mark.parametrize("precision,grid", [("fp64", (48, 32, 24)), ("mixed", (64, 64, 40)), ("mixed", (96, 48, 9)),
+                                            ("fp64dw", (64, 32, 20))])
+def test_convec_rows_matches_three_pass_form(built_lib, monkeypatch, precision, grid):
+    """The one-pass 3/2-grid x-rows of the convective term (c2r, products
+    and r2c in shared memory, spectra staged by bulk copies, levels marched
+    in chunks) against the three-pass form with the six 3/2-grid fields in
+    HBM, over steps that include the wall, the lid and the chunk
+    boundaries."""
+    from lesgo_gb300.solver import LesgoGPU
+    nx, ny, Nz = grid
+    kw = dict(nx=nx, ny=ny, Nz=Nz, dyn_init=3, cs_count=3, precision=precision)
+    monkeypatch.setenv("LESGO_CONVEC_ROWS", "0")
+    a = LesgoGPU(**kw)
+    monkeypatch.setenv("LESGO_CONVEC_ROWS", "1")
+    b = LesgoGPU(**kw)
+    for g in (a, b):
+        g.init_ic(5)
+        g.step(2)            # derivatives of a stepped field
+        g.convec()
+    # FP32: the two forms round the same arithmetic in different kernels
+    # (fused multiply-adds placed differently), a few ulps of the products;
+    # double-word: the products are formed in double-word arithmetic in the
+    # one-pass form and in FP64 from the stored 3/2-grid fields in the other
+    tol = {"fp64": 1e-14, "fp64dw": 1e-12, "mixed": 2e-5}[precision]
+    for f in ("RHSx", "RHSy", "RHSz"):
+        x, y = a.get(f)[1:a.nz, :, :nx], b.get(f)[1:b.nz, :, :nx]
+        assert np.max(np.abs(x - y)) <= tol * np.max(np.abs(x)), f
+    a.step(3)
+    b.step(3)
+    b.sync()
+    tol = {"fp64": 1e-12, "fp64dw": 1e-11, "mixed": 2e-5}[precision]
+    for f in ("u", "v", "w", "p"):
+        x, y = a.get(f)[1:a.nz, :, :nx], b.get(f)[1:b.nz, :, :nx]
+        assert np.max(np.abs(x - y)) <= tol * np.max(np.abs(x)), f
+    a.close()
+    b.close()
