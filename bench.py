@@ -72,7 +72,9 @@ def parse():
                     "instance of the batched 48-instance ensemble against the same instance alone in FP64")
     ap.add_argument("--val-steps", type=int, default=None)
     ap.add_argument("--val-window", type=int, default=2000)
-    ap.add_argument("--val-no-floor", action="store_true", help="skip the FP64 run-to-run spread (a second FP64 run)")
+    ap.add_argument("--val-no-floor", action="store_true", help="skip the FP64 run-to-run spread (a second FP64 "
+                    "ensemble)")
+    ap.add_argument("--val-members", type=int, default=None, help="realisations per side (default 3 for B, 1 for C)")
     ap.add_argument("--only-class", default=None, help="run only the ensemble's instances of one grid class, "
                     "e.g. 96x96x64 (each class is an independent batch: used to profile its launches alone)")
     return ap.parse_args()
@@ -662,17 +664,23 @@ def run_validate(args):
         turbines = wind_farm_4x3()
         steps = args.val_steps or 3000
     window = min(args.val_window, steps)
-    # the mixed side averages three realisations (the IC and u scaled by
-    # 1 +- 1e-6); a second FP64 run with u scaled by 1 + 1e-6 gives the
-    # run-to-run spread of the statistics over this window (the noise floor)
-    runs = {"fp64": long_run("fp64", steps, window, 10, 1, turbines, **kw),
-            "mixed": ensemble("mixed", steps, window, 10, 1, turbines, **kw)}
+    # Both sides are ensembles of the same size: realisations whose initial
+    # u is the IC scaled by 1 + p, p in `pert` (FP32-sized perturbations).
+    # The noise floor is a second FP64 ensemble of other perturbations
+    # against the first: the spread of the ensemble-mean statistics over
+    # this window that any two realisation sets show.
+    members = args.val_members or (3 if args.validate == "B" else 1)
+    pert = (0.0, 1e-6, -1e-6, 2e-6, -2e-6)[:members]
+    pert_floor = (3e-6, -3e-6, 4e-6, -4e-6, 5e-6)[:members]
+    runs = {"fp64": ensemble("fp64", steps, window, 10, 1, turbines, perturbs=pert, **kw),
+            "mixed": ensemble("mixed", steps, window, 10, 1, turbines, perturbs=pert, **kw)}
     nz = kw["Nz"] + 1
     r = compare(runs["mixed"], runs["fp64"], nz)
     if not args.val_no_floor:
-        fl = compare(long_run("fp64", steps, window, 10, 1, turbines, perturb=1e-6, **kw), runs["fp64"], nz)
+        fl = compare(ensemble("fp64", steps, window, 10, 1, turbines, perturbs=pert_floor, **kw), runs["fp64"], nz)
         r["fp64_noise_floor"] = {k: v for k, v in fl.items() if k in ("u_linf", "uw_linf", "power_rel")}
     r["mixed_members"] = runs["mixed"]["members"]
+    r["fp64_members"] = runs["fp64"]["members"]
     line = {"validate": args.validate, "grid": [kw["nx"], kw["ny"], kw["Nz"]], "steps": steps, "window": window,
             "nskip": 10, "samples": runs["fp64"]["samples"], "turbines": len(turbines or []),
             "bar": "u_linf <= 0.01 and uw_linf <= 0.01", "pass": r["u_linf"] <= 0.01 and r["uw_linf"] <= 0.01,
