@@ -7,7 +7,8 @@
 // and a chunk of levels, and marches up the chunk with the c2r results of
 // the levels k-1, k and k+1 held in shared memory (the products at level k
 // read w and the vorticity at k+1 and u, v at k-1).  The spectra of the
-// next level arrive by bulk copies issued one level ahead.
+// next level arrive by a bulk copy issued as soon as the current level's
+// have been read, so it runs under the current level's transforms.
 #pragma once
 #include "bulk_copy.cuh"
 #include "fft_core.cuh"
@@ -29,12 +30,12 @@ struct ConvRowsGeom {
 
 // Shared memory of a block, in complex elements: three level slots of 6 rt
 // lines (the c2r results), one scratch of 6 rt lines (the other buffer of
-// each c2r, then the two buffers of the products' r2c), and two staging
-// buffers of the raw spectra of a level (6 fields x rt rows x K modes) that
-// the bulk copies fill one level ahead; the two copy barriers follow.
+// each c2r, then the two buffers of the products' r2c), and the staging
+// buffer of the raw spectra of a level (6 fields x rt rows x K modes) that
+// the bulk copies fill; the copy barrier follows.
 __host__ __device__ inline long long conv_rows_stage_elems(int rt, int K) { return 6LL * rt * K; }
 __host__ __device__ inline long long conv_rows_smem_elems(int rt, int ls, int K) {
-  return 4LL * 6 * rt * ls + 2 * conv_rows_stage_elems(rt, K);
+  return 4LL * 6 * rt * ls + conv_rows_stage_elems(rt, K);
 }
 
 // R is the transforms' arithmetic type; the products are formed in it too.
@@ -49,8 +50,8 @@ __global__ void __launch_bounds__(256) k_convec_rows(ConvRowsGeom g, FftPlan<R> 
   const int nl3 = 3 * rt;
   const long long slot_elems = 6LL * rt * g.ls;
   T2* S = base + 3 * slot_elems;   // scratch
-  T2* stage[2] = {S + slot_elems, S + slot_elems + conv_rows_stage_elems(rt, g.K)};
-  uint64_t* bar = reinterpret_cast<uint64_t*>(stage[1] + conv_rows_stage_elems(rt, g.K));
+  T2* stage = S + slot_elems;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(stage + conv_rows_stage_elems(rt, g.K));
   const int row0 = blockIdx.x * rt;
   const int rows = min(rt, g.ny2 - row0);
   const int inst = blockIdx.z;
@@ -77,23 +78,22 @@ __global__ void __launch_bounds__(256) k_convec_rows(ConvRowsGeom g, FftPlan<R> 
   int n_entries = e_lo + e_k0;
   for (int k = k0; k < k1; ++k) n_entries += needs_next(k) ? 1 : 0;
 
-  // thread 0 arms the entry's barrier and copies its rows' spectra (one
-  // contiguous run of rows x K modes per field) into the staging buffer
+  // thread 0 arms the barrier for entry e (its phase e) and copies the
+  // entry's rows' spectra (one contiguous run of rows x K modes per field)
+  // into the staging buffer
   auto prefetch = [&](int e) {
     if (threadIdx.x != 0 || e >= n_entries) return;
     int lev, f0, nf;
     entry(e, lev, f0, nf);
     const unsigned bytes = (unsigned)(rows * g.K * sizeof(T2));
     const long long lrow = ((long long)inst * g.nz + (lev - 1)) * g.ny2 + row0;
-    mbar_arrive_expect_tx(&bar[e & 1], bytes * nf);
+    mbar_arrive_expect_tx(bar, bytes * nf);
     for (int f = 0; f < nf; ++f)
-      bulk_g2s(stage[e & 1] + (long long)(f0 + f) * rt * g.K, in + (long long)(f0 + f) * g.in_fs + lrow * g.K, bytes,
-               &bar[e & 1]);
+      bulk_g2s(stage + (long long)(f0 + f) * rt * g.K, in + (long long)(f0 + f) * g.in_fs + lrow * g.K, bytes, bar);
   };
 
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    mbar_init(bar, 1);
     mbar_init_fence();
   }
   __syncthreads();
@@ -105,16 +105,15 @@ __global__ void __launch_bounds__(256) k_convec_rows(ConvRowsGeom g, FftPlan<R> 
   auto c2r_entry = [&](int e) -> bool {
     int lev, f0, nf;
     entry(e, lev, f0, nf);
-    const bool ok = mbar_wait(&bar[e & 1], (unsigned)((e >> 1) & 1));
+    const bool ok = mbar_wait(bar, (unsigned)(e & 1));
     if (__syncthreads_or(!ok)) return false;
-    prefetch(e + 1);   // into the other buffer, whose entry e - 1 is done
     const FastDiv& fnl = nf == 6 ? g.f6 : nf == 3 ? g.f3 : g.f2;
     T2* X = base + (lev % 3) * slot_elems + (long long)f0 * rt * g.ls;
     T2* Sx = S + (long long)f0 * rt * g.ls;
     T2* A = (plan.nf & 1) ? Sx : X;
     T2* B = (plan.nf & 1) ? X : Sx;
     const int nl = nf * rt;
-    const T2* stg = stage[e & 1] + (long long)f0 * rt * g.K;
+    const T2* stg = stage + (long long)f0 * rt * g.K;
     for (int t = threadIdx.x; t < nl * H; t += blockDim.x) {
       const int l = g.fH.div(t), k = t - l * H;   // l = field offset * rt + row
       T2 z = czero<T2>();
@@ -132,6 +131,7 @@ __global__ void __launch_bounds__(256) k_convec_rows(ConvRowsGeom g, FftPlan<R> 
       A[l * g.ls + k] = z;
     }
     __syncthreads();
+    prefetch(e + 1);   // the staging buffer has been read: the next entry's copy runs under this one's stages
     fft_lines<R, true>(A, B, nl, g.ls, fnl, plan);
     return true;
   };
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) k_convec_rows(ConvRowsGeom g, FftPlan<R> 
     // only ones in flight; the next were not issued) a last bounded wait,
     // and leave
     if (threadIdx.x == 0) atomicExch(g.err, 1);
-    mbar_wait(&bar[e & 1], (unsigned)((e >> 1) & 1));
+    mbar_wait(bar, (unsigned)(e & 1));
   }
 }
 

@@ -1906,11 +1906,12 @@ class Solver : public SolverBase {
     g.out_fs = vol1_b_ * kp_.ninst;
     const int H = d_.nx2 / 2;
     // rows per block as for the other x passes, within a shared-memory
-    // budget of four blocks per SM (two for 16-byte complex values); two
-    // complex elements more hold the copy barriers
+    // budget of three blocks per SM (two for 16-byte complex values): fewer
+    // rows leave most threads idle in the radix-8 stages; one complex
+    // element more holds the copy barrier
     int rt = std::max(1, std::min(16, xtarget_ / (6 * H)));
-    auto smem_of = [&](int r) { return (size_t)(conv_rows_smem_elems(r, g.ls, d_.K) + 2) * sizeof(T2); };
-    const size_t budget = (sizeof(T2) == 16 ? 112 : 56) * 1024;
+    auto smem_of = [&](int r) { return (size_t)(conv_rows_smem_elems(r, g.ls, d_.K) + 1) * sizeof(T2); };
+    const size_t budget = (sizeof(T2) == 16 ? 112 : 74) * 1024;
     while (rt > 1 && smem_of(rt) > budget) --rt;
     g.rt = rt;
     // a chunk of at least 16 levels (each chunk repeats part of the c2r of
