@@ -1914,12 +1914,6 @@ class Solver : public SolverBase {
     const size_t budget = (sizeof(T2) == 16 ? 112 : 74) * 1024;
     while (rt > 1 && smem_of(rt) > budget) --rt;
     g.rt = rt;
-    // a chunk of at least 16 levels (each chunk repeats part of the c2r of
-    // two levels), longer chunks when the grid already fills the GPU
-    const long long tiles = (long long)((d_.ny2 + rt - 1) / rt) * kp_.ninst;
-    int cz = 16;
-    while (cz < d_.nz && tiles * ((d_.nz + cz - 1) / cz) > 8LL * 152) cz *= 2;
-    g.cz = std::min(cz, d_.nz);
     g.fH = FastDiv((unsigned)H); g.fK = FastDiv((unsigned)d_.K);
     g.f2 = FastDiv((unsigned)(2 * rt)); g.f3 = FastDiv((unsigned)(3 * rt)); g.f6 = FastDiv((unsigned)(6 * rt));
     g.frt = FastDiv((unsigned)rt);
@@ -1927,6 +1921,25 @@ class Solver : public SolverBase {
     const size_t smem = smem_of(rt);
     auto kern = k_convec_rows<A>;
     set_smem(kern, smem);
+    // Levels per chunk: every block marches its chunk (plus up to two
+    // levels of halo), so the launch takes about (waves) x (chunk + 2)
+    // level times, with waves = blocks / resident blocks.  The chunk count
+    // that minimises it keeps the last wave full (at 128^3: 7 chunks of 19
+    // levels, one wave, against 9 chunks of 16 levels in two).
+    const long long tiles = (long long)((d_.ny2 + rt - 1) / rt) * kp_.ninst;
+    int per_sm = 0, nsm = 0, dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
+    const long long slots = std::max(1LL, (long long)per_sm * nsm);
+    int best_n = 1;
+    long long best_t = -1;
+    for (int n = 1; n <= d_.nz; ++n) {
+      const long long waves = (tiles * n + slots - 1) / slots;
+      const long long t = waves * ((d_.nz + n - 1) / n + 2);
+      if (best_t < 0 || t < best_t) { best_t = t; best_n = n; }
+    }
+    g.cz = (d_.nz + best_n - 1) / best_n;
     dim3 grid((unsigned)((d_.ny2 + rt - 1) / rt), (unsigned)((d_.nz + g.cz - 1) / g.cz), (unsigned)kp_.ninst);
     pre();
     kern<<<grid, 256, smem, st_>>>(g, pxb_, cvB_, cvA_, cb);
