@@ -1850,6 +1850,7 @@ class Solver : public SolverBase {
     dst.opftdelta = 1.5 * d_.delta;
     dst.sc = sc_d_;
     dst.beta_exp = std::log(2.0) / (std::log(4.0) - std::log(2.0));
+    dst.beta_exp_one = dst.beta_exp == 1.0;
     dst.ld = d_.ld; dst.nz = d_.nz; dst.lbc = kp_.lbc; dst.ubc = kp_.ubc;
     dst.iflags = flags_d_;
     dst.plane = kp_.plane;

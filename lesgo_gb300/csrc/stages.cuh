@@ -414,6 +414,13 @@ struct DstPress {
   }
 };
 
+// x^(-1/8) for x > 0 (the Lagrangian time scale, lagrange_Sdep.f90's
+// Tn**(-1/8)): two square roots and a reciprocal square root, within a few
+// ulps of pow and far cheaper than pow in FP64, where these three powers
+// per point had bound the whole Lagrangian epilogue.
+__device__ __forceinline__ double inv_root8(double x) { return rsqrt(sqrt(sqrt(x))); }
+__device__ __forceinline__ float inv_root8(float x) { return rsqrtf(sqrtf(sqrtf(x))); }
+
 // lagrange_Sdep.f90:110-404 pointwise part: Leonard terms L, Q, model
 // tensors M, N, their contractions, the Lagrangian relaxation of F_LM,
 // F_MM, F_QN, F_NN, beta and Cs^2.  vals[2q] = quantity q at 2 Delta,
@@ -424,6 +431,7 @@ struct DstLagrange {
   const R *FLMi, *FMMi, *FQNi, *FNNi;  // interpolated running averages
   R *FLM, *FMM, *FQN, *FNN, *Cs, *Beta, *Tn_all, *ee_now;
   double cst, opftdelta, beta_exp;
+  int beta_exp_one;   // beta_exp == 1 exactly (the reference's tf1 = 2, tf2 = 4): pow(x, 1) = x
   const double* sc;   // step constants (lagran_dt)
   int ld, nz, lbc, ubc;
   const int* iflags;
@@ -466,7 +474,7 @@ struct DstLagrange {
     R fLM = FLMi[q], fMM = FMMi[q], fQN = FQNi[q], fNN = FNNi[q];
     if (init_lm) { fMM = MM; fLM = (R)0.03 * MM; }
     R Tn = max(fLM * fMM, zero);
-    Tn = (R)opftdelta * pow(Tn, (R)(-1.0 / 8.0));
+    Tn = (R)opftdelta * inv_root8(Tn);
     Tn = max(zero, Tn);
     const R ldt = (R)sc[inst * SC_N + SC_LDT];
     R dumfac = ldt / Tn;
@@ -478,7 +486,7 @@ struct DstLagrange {
     cs2d = max(zero, cs2d);
     if (init_qn) { fNN = NN; fQN = (R)0.03 * NN; }
     Tn = max(fQN * fNN, zero);
-    Tn = (R)opftdelta * pow(Tn, (R)(-1.0 / 8.0));
+    Tn = (R)opftdelta * inv_root8(Tn);
     Tn = max(zero, Tn);
     dumfac = ldt / Tn;
     epsi = dumfac / ((R)1 + dumfac);
@@ -487,7 +495,7 @@ struct DstLagrange {
     fQN = max(zero, fQN);
     R cs4d = fQN / (fNN + zero);
     cs4d = max(zero, cs4d);
-    R beta = pow(cs4d / cs2d, (R)beta_exp);
+    R beta = beta_exp_one ? cs4d / cs2d : pow(cs4d / cs2d, (R)beta_exp);
     if (k == nz && ubc == 0) beta = (R)1;
     if (k == 1 && lbc == 0) beta = (R)1;
     const R betaclip = max(beta, (R)1 / (tf1 * tf2));
