@@ -191,13 +191,32 @@ class SolverBase {
 // Whether the convective term's 3/2-grid x-rows run as one pass
 // (k_convec_rows: c2r, products and r2c in shared memory) or as three
 // (xinv to six 3/2-grid fields in HBM, products, xfwd).  One pass for the
-// mixed form, three for the FP64-field forms, whose 16-byte complex values
-// leave the one-pass kernel too few rows per block (measured slower there);
-// LESGO_CONVEC_ROWS=1 / 0 chooses for every form.
+// mixed and the double-word forms, three for the FP64 form, whose FP64
+// transforms leave the one-pass kernel slower (measured at 128^3: 8.06
+// against 7.87 ms per step); LESGO_CONVEC_ROWS=1 / 0 chooses for every form.
 static bool convec_rows_enabled(int precision) {
   const char* e = std::getenv("LESGO_CONVEC_ROWS");
   if (e) return std::strcmp(e, "0") != 0;
-  return precision == LESGO_MIXED;
+  return precision != LESGO_FP64;
+}
+
+// A kernel's dynamic shared-memory limit (cudaFuncAttributeMaxDynamicSharedMemorySize)
+// belongs to the function, not to a launch, and a replayed CUDA graph
+// launches its kernel nodes against the value current at replay.  Handles
+// of different grids share the kernel instances, so a handle that set a
+// smaller limit than another handle's captured node needs would break that
+// node's replay.  The limit is therefore only ever raised, per device,
+// under a lock (handles may live on several host threads).
+static void raise_smem_limit(const void* kern, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> limit;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& cur = limit[{dev, kern}];
+  if (bytes <= cur) return;
+  CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
 }
 
 // Device bytes of a handle (the admission footprint of a batch).
@@ -1541,10 +1560,7 @@ class Solver : public SolverBase {
   struct ProfRec { std::string name; double bytes; cudaEvent_t a, b; };
   template <typename KF>
   static void set_smem(KF kern, size_t bytes) {
-    if (bytes > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-      if (e != cudaSuccess) throw Error(LESGO_ERR_CUDA, std::string("smem attribute: ") + cudaGetErrorString(e));
-    }
+    if (bytes > 48 * 1024) raise_smem_limit(reinterpret_cast<const void*>(kern), bytes);
   }
 
   FftPlan<A> make_plan(int n) {

@@ -305,3 +305,27 @@ def test_convec_rows_matches_three_pass_form(built_lib, monkeypatch, precision, 
         assert np.max(np.abs(x - y)) <= tol * np.max(np.abs(x)), f
     a.close()
     b.close()
+
+
+def test_handles_of_different_grids_replay_together(built_lib):
+    """Handles of different grids share kernel instances whose blocks need
+    different amounts of dynamic shared memory (here the one-pass convective
+    rows: 65.7, 65.1 and 65.3 KB).  Stepped in turn with graph replay, each
+    equals its run alone bit for bit."""
+    from lesgo_gb300.solver import LesgoGPU
+    grids = [(64, 64, 16), (128, 64, 16), (96, 48, 16)]
+    kw = dict(dyn_init=3, cs_count=3, precision="mixed")
+    hs = [LesgoGPU(nx=g[0], ny=g[1], Nz=g[2], **kw) for g in grids]
+    for i, h in enumerate(hs):
+        h.init_ic(20 + i)
+    for _ in range(7):
+        for h in hs:
+            h.step(1)
+    for i, (g, h) in enumerate(zip(grids, hs)):
+        a = LesgoGPU(nx=g[0], ny=g[1], Nz=g[2], **kw)
+        a.init_ic(20 + i)
+        a.step(7)
+        for f in ("u", "w", "p"):
+            assert np.array_equal(a.get(f)[1:a.nz], h.get(f)[1:h.nz]), (g, f)
+        a.close()
+        h.close()
