@@ -140,6 +140,8 @@ struct FastDiv {
   __device__ __forceinline__ int div(int n) const {
     return d == 1 ? n : (int)(__umulhi((unsigned)n, m) >> sh);
   }
+  // the same for a divisor known to be >= 2 (no test for d = 1)
+  __device__ __forceinline__ int div2(int n) const { return (int)(__umulhi((unsigned)n, m) >> sh); }
 };
 
 // Plan for one complex FFT length n = prod(radix[]).
@@ -266,7 +268,7 @@ __device__ __forceinline__ void lines_stage(const T2* a, T2* b, int nl, int ls, 
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     const int j = fnl.div(t);
     const int l = t - j * nl;
-    const int q = FIRST ? j : fns.div(j);
+    const int q = FIRST ? j : fns.div2(j);   // after the first stage Ns >= 2
     const int jm = j - q * Ns;
     stage_bfly<T2, INV, RR, FIRST>(a + l * ls + j, b + l * ls + q * Ns * RR + jm, nb, Ns, stw + jm * (RR - 1));
   }
@@ -452,7 +454,7 @@ __device__ __forceinline__ void cols_stage(const T2* a, T2* b, int width, const 
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     const int j = fw.div(t);
     const int l = t - j * width;
-    const int q = FIRST ? j : fns.div(j);
+    const int q = FIRST ? j : fns.div2(j);   // after the first stage Ns >= 2
     const int jm = j - q * Ns;
     stage_bfly<T2, INV, RR, FIRST>(a + j * width + l, b + (q * Ns * RR + jm) * width + l, sr, sd,
                                    stw + jm * (RR - 1));
