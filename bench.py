@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--grid", type=int, default=128)
+    ap.add_argument("--e2e-split", type=int, default=3, help="batch handles per grid class in the e2e measurement "
+                    "(measured e2e: 1.75e9 with 1, 2.04e9 with 2, 2.07e9 with 3)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--forms", default="fp64,fp64dw,mixed",
                     help="single-instance 128^3 forms reported beside the ensemble (fp64dw: FP64 fields, "
@@ -211,19 +213,24 @@ def batch_instances(n=48, seed=2024):
 ONLY_CLASS = None
 
 
-def make_batches(precision="mixed"):
-    """One batch handle per grid class of the 48-instance ensemble, every
-    instance added, tile shapes autotuned."""
+def make_batches(precision="mixed", split=1):
+    """Batch handles of the 48-instance ensemble, every instance added, tile
+    shapes autotuned: one per grid class, or `split` per class (the class's
+    instances dealt in turn)."""
     from lesgo_gb300.solver import LesgoBatch
     by_grid = {}
     for g, zo, seed in batch_instances():
         by_grid.setdefault(g, []).append((zo, seed))
     batches = []
     for g, lst in by_grid.items():
-        b = LesgoBatch(len(lst), nx=g[0], ny=g[1], Nz=g[2], precision=precision, dyn_init=5, cs_count=5)
-        ids = [b.add(zo, seed) for zo, seed in lst]
-        b.autotune()
-        batches.append((g, ids, b))
+        for part in range(split):
+            sub = lst[part::split]
+            if not sub:
+                continue
+            b = LesgoBatch(len(sub), nx=g[0], ny=g[1], Nz=g[2], precision=precision, dyn_init=5, cs_count=5)
+            ids = [b.add(zo, seed) for zo, seed in sub]
+            b.autotune()
+            batches.append((g, ids, b))
     return batches
 
 
@@ -326,8 +333,10 @@ def time_e2e_batched(args, torch):
     classes step once, and u, v, w of every instance come back.  The copies
     are queued in stream order (the *_async calls): each class's copies run
     on its handle's stream while the other classes' steps run, and a step's
-    uploads read the buffers its predecessor's downloads wrote."""
-    batches = make_batches("mixed")
+    uploads read the buffers its predecessor's downloads wrote.  With
+    `--e2e-split` handles per class, one handle's copies also run while the
+    other handles of its class step."""
+    batches = make_batches("mixed", split=args.e2e_split)
     step_all(batches, 10)
     host = []
     nbytes = 0
