@@ -137,7 +137,8 @@ def _farm(nxr=2, nyr=2):
     return ts, farm
 
 
-def test_turbines_fp64(built_lib):
+@pytest.mark.parametrize("precision", ["fp64", "fp64dw"])
+def test_turbines_fp64(built_lib, precision):
     """Actuator-disk forcing (turbines.f90:465-638) against the oracle: forces
     after the first step, and fields and per-turbine power after 6 steps."""
     from oracle.lesgo_oracle import Oracle, Params
@@ -147,8 +148,9 @@ def test_turbines_fp64(built_lib):
     o = Oracle(p)
     o.set_ic(3)
     from lesgo_gb300.solver import LesgoGPU
-    g = LesgoGPU(turbines=ts, **kw)
+    g = LesgoGPU(turbines=ts, precision=precision, **kw)
     g.init_ic(3)
+    force_tol = 1e-12 if precision == "fp64" else 1e-11
     for step in range(6):
         for name, fn, outs in o.stages():
             fn()
@@ -156,7 +158,7 @@ def test_turbines_fp64(built_lib):
             if step == 0 and name == "turbines_forcing":
                 for f in ("fxa", "fza"):
                     e = rel_err(p, f, g.get(f), getattr(o, f))
-                    assert e < 1e-12, (f, e)
+                    assert e < force_tol, (f, e)
     for f in ("u", "v", "w", "p"):
         e = rel_err(p, f, g.get(f), oracle_field(o, f))
         assert e < STEP_TOL, (f, e)
@@ -164,7 +166,7 @@ def test_turbines_fp64(built_lib):
     po = o.turbine_power()
     assert np.max(np.abs(ps - po)) / np.max(np.abs(po)) < 1e-10
     # the fused step agrees with the drop-in sequence
-    g2 = LesgoGPU(turbines=ts, **kw)
+    g2 = LesgoGPU(turbines=ts, precision=precision, **kw)
     g2.init_ic(3)
     g2.step(6)
     for f in ("u", "w"):
@@ -175,13 +177,13 @@ def test_turbines_fp64(built_lib):
 def test_batch_alone_equals_mixed(built_lib):
     """Each instance of a batch (own roughness and seed, one with actuator
     disks) equals the same instance run alone: fields identical bit for bit
-    in FP64 and in the mixed form, including an instance admitted late and
-    after a removal compacted the batch."""
+    in every precision form, including an instance admitted late and after
+    a removal compacted the batch."""
     from lesgo_gb300.solver import LesgoBatch, LesgoGPU
     ts, _ = _farm(1, 2)
     base = dict(nx=32, ny=32, Nz=24, dyn_init=3, cs_count=3)
     specs = [(1e-4, 11, None), (3e-5, 12, ts), (8e-4, 13, None)]
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "fp64dw", "mixed"):
         b = LesgoBatch(capacity=4, precision=prec, **base)
         ids = [b.add(zo, seed, tb) for zo, seed, tb in specs]
         b.step(4)

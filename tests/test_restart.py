@@ -93,7 +93,7 @@ BASE = dict(nx=32, ny=32, Nz=16, dyn_init=3, cs_count=3)
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "fp64dw", "mixed"])
 def test_gpu_restart_is_bitwise(built_lib, tmp_path, precision):
     """10 steps straight == 5 steps, checkpoint, restart in a new handle, 5 steps."""
     from lesgo_gb300.solver import LesgoGPU

@@ -113,7 +113,7 @@ def _compare(p, ta, get, prof, tol, names=TAVG_NAMES + TAVG_RS_NAMES):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-3)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp64dw", 1e-10), ("mixed", 1e-3)])
 def test_gpu_tavg_matches_oracle(built_lib, precision, tol):
     from gpu_util import make_pair
     p, o, g = make_pair(precision=precision, nx=32, ny=32, Nz=32, dyn_init=5)
