@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--val-no-floor", action="store_true", help="skip the FP64 run-to-run spread (a second FP64 "
                     "ensemble)")
     ap.add_argument("--val-members", type=int, default=None, help="realisations per side (default 3 for B, 1 for C)")
+    ap.add_argument("--xdft-compare", action="store_true", help="the forward x transforms as tensor-core GEMMs "
+                    "(LESGO_XDFT=1) against the radix kernels: per-stage and whole-step times")
     ap.add_argument("--only-class", default=None, help="run only the ensemble's instances of one grid class, "
                     "e.g. 96x96x64 (each class is an independent batch: used to profile its launches alone)")
     return ap.parse_args()
@@ -702,6 +704,72 @@ def run_validate(args):
     print(json.dumps(line), flush=True)
 
 
+def run_xdft_compare(args):
+    """The forward x transforms as tensor-core GEMMs (k_xdft_tc: three-pass
+    TF32 splitting, FP32 accuracy; LESGO_XDFT=1) against the radix kernels
+    (k_xfwd), in the mixed form: the x-forward stages' CUDA-event times and
+    achieved algorithmic GB/s, and the whole step's device time, for one
+    128^3 instance and for the 48-instance ensemble.  Both arms run the same
+    instances from the same seeds; the tiles are autotuned per arm."""
+    import torch
+    torch.cuda.set_device(0)
+    from lesgo_gb300.solver import LesgoGPU
+    hbm = peaks()[0]
+    warm, steps = timed_steps(args)
+
+    def xf_stages(rep):
+        out = {}
+        for k, (n, ms, by) in rep.items():
+            if k.endswith("xfwd"):
+                out[k] = dict(launches=n, us_per_launch=1e3 * ms / n, gbs=by / (ms * 1e-3) / 1e9 if ms > 0 else 0.0,
+                              frac_of_measured_hbm=(by / (ms * 1e-3) / 1e9) / hbm if ms > 0 else 0.0)
+        return out
+
+    res = {}
+    for mode in ("0", "1"):
+        os.environ["LESGO_XDFT"] = mode
+        n = args.grid
+        g = LesgoGPU(**dict(WORKLOAD, nx=n, ny=n, Nz=n, precision="mixed"))
+        g.init_ic(1)
+        g.autotune()
+        g.step(warm)
+        ms1 = timed_on_device(torch, [(None, None, g)], lambda: g.step(steps))
+        g.profile(True)
+        g.step(5)
+        rep1 = g.profile_report()
+        g.profile(False)
+        u1 = g.get("u")
+        g.close()
+        batches = make_batches("mixed")
+        step_all(batches, warm)
+        msb = timed_on_device(torch, batches, lambda: step_all(batches, steps))
+        reps = []
+        for _, _, b in batches:
+            b.profile(True)
+            b.step(5)
+            reps.append(b.profile_report())
+            b.profile(False)
+        for _, _, b in batches:
+            b.close()
+        repb = merge_profiles(reps)
+        res[mode] = dict(single_ms_per_step=ms1 / steps, ensemble_ms_per_step=msb / steps,
+                         single_xfwd=xf_stages(rep1), ensemble_xfwd=xf_stages(repb),
+                         single_xfwd_ms_per_step=sum(v[1] for k, v in rep1.items() if k.endswith("xfwd")) / 5,
+                         ensemble_xfwd_ms_per_step=sum(v[1] for k, v in repb.items() if k.endswith("xfwd")) / 5,
+                         u=u1)
+    du = float(abs(res["1"]["u"] - res["0"]["u"]).max() / abs(res["0"]["u"]).max())
+    for r in res.values():
+        del r["u"]
+    line = {"xdft_compare": True, "grid": args.grid, "warmup": warm, "steps": steps, "hbm_gbs_measured": hbm,
+            "radix": res["0"], "tensor_core_gemm": res["1"],
+            "single_u_max_rel_diff_after_warmup_and_timed_steps": du,
+            "xfwd_speedup_single": res["0"]["single_xfwd_ms_per_step"] / res["1"]["single_xfwd_ms_per_step"],
+            "xfwd_speedup_ensemble": res["0"]["ensemble_xfwd_ms_per_step"] / res["1"]["ensemble_xfwd_ms_per_step"],
+            "step_speedup_single": res["0"]["single_ms_per_step"] / res["1"]["single_ms_per_step"],
+            "step_speedup_ensemble": res["0"]["ensemble_ms_per_step"] / res["1"]["ensemble_ms_per_step"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global ONLY_CLASS
     args = parse()
@@ -712,6 +780,8 @@ def main():
         run_validate(args)
     elif args.serve:
         run_serve(args)
+    elif args.xdft_compare:
+        run_xdft_compare(args)
     else:
         run_ours(args)
 

@@ -8,6 +8,7 @@
 #include "lesgo_gpu.h"
 #include "kernels.cuh"
 #include "convec_rows.cuh"
+#include "tc_dft.cuh"
 #include "restart_io.hpp"
 #include "conf.hpp"
 
@@ -324,6 +325,14 @@ class Solver : public SolverBase {
       thomas_mode_ = std::strcmp(e, "seq") == 0 ? 1 : std::strcmp(e, "seg") == 0 ? 2 : 0;
     use_graphs_ = graphs_allowed_;
     build_tables();
+    // x-direction forward transforms as tensor-core GEMMs (FP32 transforms,
+    // nx a multiple of 16 up to 128): LESGO_XDFT=1
+    if (std::is_same<A, float>::value && nx % 16 == 0 && nx <= 128)
+      if (const char* e = std::getenv("LESGO_XDFT"); e && std::strcmp(e, "1") == 0) {
+        const std::vector<float> img = xdft_image(nx);
+        xdft_w_ = alloc<float>((long long)img.size());
+        CK(cudaMemcpyAsync(xdft_w_, img.data(), img.size() * sizeof(float), cudaMemcpyHostToDevice, st_));
+      }
     CK(cudaStreamSynchronize(st_));
   }
 
@@ -1706,6 +1715,12 @@ class Solver : public SolverBase {
   template <int NF, class Src>
   void xfwd(const Src& src, int M, int nyrows, int nli, T2* out, const FftPlan<A>& plan, const char* tag = "xfwd",
             int in_fields = NF) {
+    if constexpr (std::is_same<T2, float2>::value && std::is_same<typename Src::C, float2>::value) {
+      if (xdft_w_ && M == d_.nx) {
+        xfwd_tc<NF>(src, M, nyrows, nli, out, tag, in_fields);
+        return;
+      }
+    }
     XfGeom g;
     g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nli * kp_.ninst; g.ls = M / 2 + 1;
     const int target = xtarget_;
@@ -1719,6 +1734,35 @@ class Solver : public SolverBase {
     set_smem(kern, smem);
     pre();
     kern<<<(g.nrows + g.rpc - 1) / g.rpc, 256, smem, st_>>>(g, plan, src, out);
+    post(tag, (double)g.nrows * ((double)in_fields * M * sizeof(R) + (double)NF * g.K * sizeof(T2)));
+  }
+
+  // The same transform as a tensor-core GEMM (k_xdft_tc): tiles of 128 rows,
+  // one persistent block per SM (its shared memory holds W).
+  template <int NF, class Src>
+  void xfwd_tc(const Src& src, int M, int nyrows, int nli, float2* out, const char* tag, int in_fields) {
+    XdGeom g{};
+    g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nli * kp_.ninst;
+    g.rpc = 128 / NF;
+    g.ntiles = (g.nrows + g.rpc - 1) / g.rpc;
+    g.pcols = (unsigned)((M + 31) / 32 * 32);
+    g.ncols = 4 * g.pcols <= 128 ? 128u : 4 * g.pcols <= 256 ? 256u : 512u;
+    g.out_field_stride = (long long)g.nrows * g.K;
+    g.fnyrows = FastDiv((unsigned)nyrows);
+    g.err = err_ + 1;
+    // Blocks that share an SM must never ask for more than its 512
+    // tensor-memory columns (an allocation would wait): enough shared
+    // memory per block keeps their number at 512 / ncols or fewer.
+    const size_t smem = std::max<size_t>(xdft_smem(M), g.ncols == 512 ? 116 * 1024 : g.ncols == 256 ? 78 * 1024 : 58 * 1024);
+    if (smem > 227 * 1024) throw Error(LESGO_ERR_UNSUPPORTED, "x transform GEMM: shared memory");
+    auto kern = k_xdft_tc<NF, Src>;
+    set_smem(kern, smem);
+    int nsm = 0, dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = std::min(g.ntiles, nsm);
+    pre();
+    kern<<<grid, kXdThreads, smem, st_>>>(g, xdft_w_, src, out);
     post(tag, (double)g.nrows * ((double)in_fields * M * sizeof(R) + (double)NF * g.K * sizeof(T2)));
   }
 
@@ -2181,6 +2225,7 @@ class Solver : public SolverBase {
   bool prof_on_ = false;
   bool branches_allowed_ = true;   // LESGO_BRANCHES=0: the fused step on one stream
   bool conv_rows_ = false;         // the one-pass 3/2-grid x-rows of the convective term
+  float* xdft_w_ = nullptr;        // DFT matrix images of the tensor-core x transform (when enabled)
   cudaEvent_t prof_start_ = nullptr;
   std::vector<ProfRec> prof_;
   std::map<int, cudaGraphExec_t> graphs_;
