@@ -498,7 +498,11 @@ __device__ cplx<R>* fft_cols(cplx<R>* a, cplx<R>* b, int width, const FastDiv& f
 // truncation), inverse transformed if INV, and stored.  Op supplies
 // pointers, coefficients and the row map.  Tiles are row-major: input i,
 // row y, column c at S[y * NIN * tk + i * tk + c]; outputs W[y * tk + c].
-template <typename R, int NIN, int NOUT, bool FWD, bool INV, class Op>
+//
+// SC compiles in the transform-free path of kx-only outputs (the host picks
+// the instance with it only for passes that have such an output, so that
+// the other passes keep their register count).
+template <typename R, int NIN, int NOUT, bool FWD, bool INV, bool SC, class Op>
 __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<R> pout, Op op) {
   using T2 = cplx<R>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -535,8 +539,90 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
     }
   }
   __syncthreads();
-  if (FWD) fft_cols<R, false>(L, L == S ? X : S, win, g.fwin, pin);   // ends in S
+  // What each output needs on this tile (the same in every thread): 0 the
+  // transforms, 1 none (its operator depends on kx alone), 2 the inverse
+  // result of another output times i kx, 3 nothing (zero on this tile).
+  // (Only the instances that can meet kinds 1-3 compile their paths: kx-only
+  // outputs with SC, zero tiles in the one-input forward-inverse passes (the
+  // test filters), derived outputs in the inverse-only passes.)
+  constexpr bool kZero = FWD && INV && NIN == 1;
+  constexpr bool kDerive = !FWD && INV;
+  constexpr bool kPlain = !SC && !kZero && !kDerive;   // every output takes the transforms
+  int kind[NOUT];
+  bool need_fwd = kPlain, any_sc = false;
+  if constexpr (!kPlain) {
+#pragma unroll
+    for (int o = 0; o < NOUT; ++o) {
+      kind[o] = 0;
+      if constexpr (kDerive) if (op.from[o] >= 0) kind[o] = 2;
+      if constexpr (kZero) if (kx0 >= op.zero_from[o]) kind[o] = 3;
+      if constexpr (SC) if (kind[o] == 0 && op.sc_out[o]) kind[o] = 1;
+      need_fwd |= kind[o] == 0;
+      any_sc |= kind[o] == 1;
+    }
+  }
+  if constexpr (SC) if (any_sc) {
+    // A forward and inverse y transform with the y Nyquist row zeroed
+    // between them is, per column, ny x(y) - (-1)^y s with
+    // s = sum_l (-1)^l x(l) (the Nyquist component removed); a kx-only
+    // operator then multiplies every row alike.  Partial sums of s over
+    // each thread's rows go to the buffer the forward transform has not
+    // loaded into.
+    T2* F = (L == S) ? X : S;
+    const int nr = min(rstep, g.ny_in);
+    if (r0 < nr) {
+#pragma unroll
+      for (int i = 0; i < NIN; ++i) {
+        T2 acc = czero<T2>();
+        for (int jy = r0; jy < g.ny_in; jy += rstep) {
+          const T2 v = L[jy * win + i * g.tk + c];
+          acc = (jy & 1) ? csub(acc, v) : cadd(acc, v);
+        }
+        F[r0 * win + i * g.tk + c] = acc;
+      }
+    }
+    __syncthreads();
+    T2 sn[NIN];
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) {
+      T2 acc = czero<T2>();
+      for (int r = 0; r < nr; ++r) acc = cadd(acc, F[r * win + i * g.tk + c]);
+      sn[i] = acc;
+    }
+    const R nyr = cvt<R>((double)g.ny_in);
+    for (int o = 0; o < NOUT; ++o) {
+      if (kind[o] != 1) continue;
+      auto* dst = op.out_plane(grp, o, li) + kx;
+      using OutT = typename std::remove_pointer<decltype(dst)>::type;
+#pragma unroll 2
+      for (int jy = r0; jy < g.ny_out; jy += rstep) {
+        T2 acc = czero<T2>();
+#pragma unroll
+        for (int i = 0; i < NIN; ++i) {
+          const T2 v = L[jy * win + i * g.tk + c];
+          const T2 sv = mkc(v.x * nyr, v.y * nyr);
+          const T2 t = (jy & 1) ? cadd(sv, sn[i]) : csub(sv, sn[i]);
+          T2 cf;
+          if (op.is_one(o, i)) acc = cadd(acc, t);
+          else if (op.coef(grp, o, i, kx, 0, cf)) acc = cadd(acc, cmul(t, cf));
+        }
+        if (live) dst[(long long)jy * g.K] = cvt2<OutT>(acc);
+      }
+    }
+    __syncthreads();   // F is the forward transform's scratch
+  }
+  if (FWD && need_fwd) fft_cols<R, false>(L, L == S ? X : S, win, g.fwin, pin);   // ends in S
   for (int o = 0; o < NOUT; ++o) {
+    if constexpr (!kPlain) if (kind[o] == 1 || kind[o] == 2) continue;
+    if constexpr (kZero) if (kind[o] == 3) {
+      if (live) {
+        auto* dst = op.out_plane(grp, o, li) + kx;
+        using OutT = typename std::remove_pointer<decltype(dst)>::type;
+        const OutT z{};
+        for (int ky = r0; ky < g.ny_out; ky += rstep) dst[(long long)ky * g.K] = z;
+      }
+      continue;
+    }
 #pragma unroll 2
     for (int ky = r0; ky < g.ny_out; ky += rstep) {
       T2 acc = czero<T2>();
@@ -561,6 +647,17 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
 #pragma unroll 4
       for (int ky = r0; ky < g.ny_out; ky += rstep) {
         dst[(long long)ky * g.K] = cvt2<OutT>(res[ky * g.tk + c]);
+      }
+      // outputs that are i kx times this one (inverse passes: the transform
+      // is linear and kx is constant on a column)
+      if constexpr (kDerive) for (int o2 = o + 1; o2 < NOUT; ++o2) {
+        if (kind[o2] != 2 || op.from[o2] != o) continue;
+        T2 cf;
+        op.coef(grp, o2, op.from_in[o2], kx, 0, cf);
+        auto* d2 = op.out_plane(grp, o2, li) + kx;
+#pragma unroll 4
+        for (int ky = r0; ky < g.ny_out; ky += rstep)
+          d2[(long long)ky * g.K] = cvt2<OutT>(cmul(res[ky * g.tk + c], cf));
       }
     }
     __syncthreads();

@@ -321,6 +321,7 @@ class Solver : public SolverBase {
     if (const char* e = std::getenv("LESGO_XTARGET")) xtarget_ = std::max(256, std::atoi(e));
     if (const char* e = std::getenv("LESGO_YBUDGET")) ybudget_ = (size_t)std::max(8192, std::atoi(e));
     if (const char* e = std::getenv("LESGO_YTHREADS")) ythreads_ = std::atoi(e) == 128 ? 128 : 256;
+    if (const char* e = std::getenv("LESGO_YSHORTCUT")) yshort_ = std::strcmp(e, "0") != 0;
     if (const char* e = std::getenv("LESGO_THOMAS"))
       thomas_mode_ = std::strcmp(e, "seq") == 0 ? 1 : std::strcmp(e, "seg") == 0 ? 2 : 0;
     use_graphs_ = graphs_allowed_;
@@ -1691,6 +1692,15 @@ class Solver : public SolverBase {
     kyw64_ = upload_as<double>(ky);
     G1_ = upload_as<A>(G1);
     G2_ = upload_as<A>(G2);
+    // the test filters vanish on every column past the cutoff circle: the y
+    // pass writes zeros there without transforming
+    for (int f = 0; f < 2; ++f) {
+      const std::vector<double>& G = f == 0 ? G1 : G2;
+      kmax_g_[f] = -1;
+      for (int jy = 0; jy < ny; ++jy)
+        for (int jx = 0; jx < lh; ++jx)
+          if (G[(size_t)jy * lh + jx] != 0.0) kmax_g_[f] = std::max(kmax_g_[f], jx);
+    }
   }
   template <typename T>
   T* upload_as(const std::vector<double>& v) {
@@ -1808,6 +1818,43 @@ class Solver : public SolverBase {
       ++o;
     }
     op.kxw = kxw_; op.kyw = kyw_; op.G1 = G1_; op.G2 = G2_;
+    for (int o = 0; o < NOUT; ++o) {
+      // zero from the first column past its test filters' cutoffs (or never)
+      int zf = -1;
+      bool kxonly = true;
+      for (int i = 0; i < NIN; ++i) {
+        const int m = op.mul[o][i];
+        if (m == MUL_ZERO) continue;
+        if (m != MUL_ONE && m != MUL_IKX) kxonly = false;
+        if (m == MUL_G1 || m == MUL_G2) zf = std::max(zf, kmax_g_[m == MUL_G1 ? 0 : 1] + 1);
+        else zf = 1 << 30;
+      }
+      op.zero_from[o] = zf < 0 ? 0 : zf;
+      op.sc_out[o] = kxonly && zf >= 0;
+      if (!yshort_) { op.zero_from[o] = 1 << 30; op.sc_out[o] = false; }
+    }
+    // inverse-only passes: an output that is i kx times an earlier output
+    // (MUL_IKX where the earlier one has MUL_ONE, zero elsewhere) takes the
+    // earlier output's inverse transform
+    for (int o2 = 0; o2 < NOUT; ++o2) {
+      op.from[o2] = -1;
+      op.from_in[o2] = 0;
+    }
+    if constexpr (!FWD && INV) {
+      for (int o2 = 0; o2 < NOUT && rowmode == ROW_SAME && yshort_; ++o2) {
+        for (int o1 = 0; o1 < o2 && op.from[o2] < 0; ++o1) {
+          bool match = true, any = false;
+          int fin = 0;
+          for (int i = 0; i < NIN; ++i) {
+            const int a = op.mul[o1][i], b = op.mul[o2][i];
+            if (a == MUL_ZERO && b == MUL_ZERO) continue;
+            if (a == MUL_ONE && b == MUL_IKX) { any = true; fin = i; continue; }
+            match = false;
+          }
+          if (match && any && op.from[o1] < 0) { op.from[o2] = o1; op.from_in[o2] = fin; }
+        }
+      }
+    }
     YGeom g;
     g.ny_in = in_rows; g.ny_out = out_rows; g.K = d_.K; g.nlev = nlev;
     g.ls_in = in_rows + 1; g.ls_out = out_rows + 1;
@@ -1830,11 +1877,26 @@ class Solver : public SolverBase {
     g.ftk = FastDiv((unsigned)tk);
     g.in_lev_stride = 0; g.out_lev_stride = 0;
     const size_t smem = smem_of(tk);
-    auto kern = k_ypass<A, NIN, NOUT, FWD, INV, YOpLin<A, NIN, NOUT, InT, OutT>>;
-    set_smem(kern, smem);
     dim3 grid((d_.K + tk - 1) / tk, nlev, ngroups);
-    pre();
-    kern<<<grid, ythreads_, smem, st_>>>(g, pin, pout, op);
+    // an output whose operator depends on kx alone needs no y transform:
+    // the instance with that path, for the one-input passes that have one
+    bool sc = false;
+    if constexpr (FWD && INV && NIN == 1) {
+      if (rowmode == ROW_SAME && in_rows == out_rows)
+        for (int o = 0; o < NOUT; ++o) sc |= op.sc_out[o];
+      if (sc) {
+        auto kern = k_ypass<A, NIN, NOUT, FWD, INV, true, YOpLin<A, NIN, NOUT, InT, OutT>>;
+        set_smem(kern, smem);
+        pre();
+        kern<<<grid, ythreads_, smem, st_>>>(g, pin, pout, op);
+      }
+    }
+    if (!sc) {
+      auto kern = k_ypass<A, NIN, NOUT, FWD, INV, false, YOpLin<A, NIN, NOUT, InT, OutT>>;
+      set_smem(kern, smem);
+      pre();
+      kern<<<grid, ythreads_, smem, st_>>>(g, pin, pout, op);
+    }
     post(tag, (double)ngroups * nlev * d_.K *
                   ((double)NIN * in_rows * sizeof(InT) + (double)NOUT * out_rows * sizeof(OutT)));
   }
@@ -2197,6 +2259,7 @@ class Solver : public SolverBase {
   int xtarget_ = 2048;
   size_t ybudget_ = sizeof(T2) == 16 ? 110 * 1024 : 48 * 1024;
   int ythreads_ = 256;   // y-pass block size (a multiple of the tile width)
+  bool yshort_ = true;   // y-pass outputs without transforms where the operator allows (k_ypass)
   int thomas_mode_ = 0;   // 0 by column count, 1 sequential, 2 segmented
   int dlog_cap_ = 0, dlog_every_ = 0;
   long long tacc_stride_ = 0;
@@ -2210,6 +2273,7 @@ class Solver : public SolverBase {
   long long staging_n_ = 0;
   FftPlan<A> px_{}, py_{}, pxb_{}, pyb_{};
   A *kxw_ = nullptr, *kyw_ = nullptr, *G1_ = nullptr, *G2_ = nullptr;
+  int kmax_g_[2] = {1 << 30, 1 << 30};   // largest kx column with a nonzero G1 / G2 weight
   double *kxw64_ = nullptr, *kyw64_ = nullptr;
   TurbineHost th_;
   TurbDev td_{};

@@ -240,6 +240,13 @@ struct YOpLin {
   int K, lh, ny_small, ny_big, rowmode;
   int mul[NOUT][NIN];
   const R *kxw, *kyw, *G1, *G2;
+  // per output, set by the host (k_ypass): the first kx from which it is
+  // zero (test-filter terms only), whether its operator depends on kx alone,
+  // and (inverse-only passes) the output it is i kx times (-1: none) with an
+  // input whose multiplier in it is MUL_IKX
+  int zero_from[NOUT];
+  bool sc_out[NOUT];
+  int from[NOUT], from_in[NOUT];
 
   // row 0, column 0 of input i of group g at launch level li (rows K apart)
   __device__ __forceinline__ const InT* in_plane(int g, int i, int li) const {
@@ -265,6 +272,8 @@ struct YOpLin {
   }
   // a plain copy of input i into output o (no multiply)
   __device__ __forceinline__ bool is_one(int o, int i) const { return mul[o][i] == MUL_ONE; }
+  __device__ __forceinline__ bool same_rows() const { return rowmode == ROW_SAME; }
+
   __device__ __forceinline__ bool coef(int g, int o, int i, int kx, int kin, cplx<R>& cf) const {
     switch (mul[o][i]) {
       case MUL_ONE: cf = mkc(FftConst<R>::one(), FftConst<R>::zero()); return true;

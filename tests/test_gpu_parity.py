@@ -331,3 +331,28 @@ def test_handles_of_different_grids_replay_together(built_lib):
             assert np.array_equal(a.get(f)[1:a.nz], h.get(f)[1:h.nz]), (g, f)
         a.close()
         h.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64dw", "mixed"])
+def test_y_pass_shortcuts_match_transforms(built_lib, monkeypatch, precision):
+    """The y pass's transform-free outputs (kx-only operators: the filtered
+    field and its x derivative; the pressure's x derivative from its
+    inverse transform; test-filter outputs on tiles past the cutoff) against
+    the same steps with every output transformed (LESGO_YSHORTCUT=0), over
+    steps with two dynamic-model updates."""
+    from lesgo_gb300.solver import LesgoGPU
+    kw = dict(nx=64, ny=48, Nz=24, dyn_init=3, cs_count=3, precision=precision)
+    monkeypatch.setenv("LESGO_YSHORTCUT", "0")
+    a = LesgoGPU(**kw)
+    monkeypatch.delenv("LESGO_YSHORTCUT")
+    b = LesgoGPU(**kw)
+    for g in (a, b):
+        g.init_ic(9)
+        g.step(7)
+        g.sync()
+    tol = {"fp64": 1e-13, "fp64dw": 1e-11, "mixed": 2e-5}[precision]
+    for f in ("u", "v", "w", "p", "F_LM", "F_MM"):
+        x, y = a.get(f)[1:a.nz, :, :64], b.get(f)[1:b.nz, :, :64]
+        assert np.max(np.abs(x - y)) <= tol * np.max(np.abs(x)), (f, np.max(np.abs(x - y)) / np.max(np.abs(x)))
+    a.close()
+    b.close()
