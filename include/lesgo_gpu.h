@@ -209,8 +209,9 @@ int lesgo_gpu_tridag_array(lesgo_handle_t* h, const double* a, const double* b, 
  * hold no handle): it needs no handle and allocates nothing.  Scratch is a
  * fixed 16 MiB array inside the library (lh*ny*n <= 2^21 doubles; larger
  * problems get LESGO_ERR_ARG), held on every GPU that loads the library.
- * The first call on a device looks up that array's address (make it
- * outside stream capture).  Calls share the array: calls whose GPU work
+ * Never capturable: each call waits for its own result, so a call on a
+ * capturing stream returns LESGO_ERR_ARG and queues nothing (the capture
+ * stays intact).  Calls share the array: calls whose GPU work
  * overlaps race.  Launches on `stream` (NULL: default stream) and returns
  * when done; LESGO_ERR_NUMERIC on a zero pivot.  After a nonzero return,
  * lesgo_gpu_last_error(NULL) describes the failure; a successful call does

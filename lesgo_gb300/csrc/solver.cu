@@ -268,8 +268,10 @@ extern "C" int lesgo_gpu_tridag_array(lesgo_handle_t* h, const double* a, const 
 // doubles (16 MiB); every GPU that loads the library holds it until the
 // process exits.  Host code may not use the array's name as a device
 // address, so the first call on each device looks the address up with
-// cudaGetSymbolAddress while that device is current and caches it; make that
-// first call outside any stream capture.  All calls on a device share the
+// cudaGetSymbolAddress while that device is current and caches it.  No call
+// can be captured in a CUDA graph (each waits for its own result): a call on
+// a capturing stream returns LESGO_ERR_ARG without queueing anything.  All
+// calls on a device share the
 // array and it keeps the previous call's contents (the solve writes every
 // scratch entry before reading it; the error flag is cleared each call), so
 // calls whose GPU work overlaps in time race on it: issue them in order, on
@@ -299,8 +301,18 @@ extern "C" int lesgo_gpu_tridag_array_noalloc(const double* a, const double* b, 
     return noalloc_fail(LESGO_ERR_ARG, "tridag_array_noalloc: lh*ny*n = " + std::to_string(need) +
                                            " exceeds the fixed scratch of " + std::to_string(kTridagScratchDoubles) +
                                            " doubles");
+  // the call reads its pivot flag back and waits for the stream, which a
+  // capturing stream cannot do: refuse before queueing anything, so that
+  // the caller's capture stays intact
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing((cudaStream_t)stream, &cap);
+  if (e != cudaSuccess)
+    return noalloc_fail(LESGO_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return noalloc_fail(LESGO_ERR_ARG, "tridag_array_noalloc: the stream is capturing; the call waits for its "
+                                       "result, so it cannot be captured");
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(LESGO_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   NoAllocSlot slot;
   {

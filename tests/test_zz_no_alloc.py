@@ -80,3 +80,24 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(built_lib):
                                            C.c_void_p(16), 129, 256, 194, None)
     assert rc == _lib.LESGO_ERR_ARG
     assert b"exceeds the fixed scratch" in lib.lesgo_gpu_last_error(None)
+
+
+def test_noalloc_refuses_a_capturing_stream_and_keeps_the_capture(built_lib):
+    """The call waits for its own result, so it cannot be captured: on a
+    capturing stream it returns LESGO_ERR_ARG before queueing anything, and
+    the caller's capture still ends and replays."""
+    import torch
+    from lesgo_gb300 import _lib
+    lib = _lib.load()
+    x = torch.zeros(4, device="cuda")
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        x.add_(1.0)
+        rc = lib.lesgo_gpu_tridag_array_noalloc(C.c_void_p(16), C.c_void_p(16), C.c_void_p(16), C.c_void_p(16),
+                                               C.c_void_p(16), 5, 4, 6,
+                                               C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == _lib.LESGO_ERR_ARG
+    assert b"capturing" in lib.lesgo_gpu_last_error(None)
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.all(x == 1.0)   # the captured add ran once, in the replay
