@@ -111,6 +111,13 @@ template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { return m
 template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
   return mkc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+// FP32 complex adds as Blackwell's packed FP32x2 instructions (one issue
+// slot for both components; each component rounds as __fadd_rn / __fmaf_rn):
+// the transforms are bound by instruction issue
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) { return __fadd2_rn(a, b); }
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);   // a - b, exact product by -1
+}
 template <typename T2> __device__ __forceinline__ T2 cmulconj(T2 a, T2 b) {  // a * conj(b)
   return mkc(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
