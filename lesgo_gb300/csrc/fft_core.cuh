@@ -388,6 +388,7 @@ struct XiGeom {
   int ls;
   long long in_field_stride;
   FastDiv fH, fM, fnyrows, frpc, fnl;   // by M/2, M, nyrows, rpc, NF * rpc
+  int kz0, kz1;   // modes kx >= kz0 (even fields) / kz1 (odd fields) are zero and not read (K: none)
 };
 
 // Xi: c2r along x for NF fields at once, then Dst::store(jy, li, i, vals)
@@ -411,9 +412,10 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
     T2 z = czero<T2>();
     if (row < g.nrows) {
       const T2* src = in + (long long)f * g.in_field_stride + (long long)row * g.K;
-      T2 xk = k < g.K ? src[k] : czero<T2>();
+      const int kzf = (f & 1) ? g.kz1 : g.kz0;   // a select: no indexing into the parameter block
+      T2 xk = k < kzf ? src[k] : czero<T2>();
       const int km = H - k;   // k = 0 -> Nyquist (zero)
-      T2 xm = (k > 0 && km < g.K) ? src[km] : czero<T2>();
+      T2 xm = (k > 0 && km < kzf) ? src[km] : czero<T2>();
       T2 a = mkc(xk.x + xm.x, xk.y - xm.y);
       T2 b = mkc(xk.x - xm.x, xk.y + xm.y);
       T2 w = ldt(plan.rtw + k);
@@ -622,7 +624,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
   for (int o = 0; o < NOUT; ++o) {
     if constexpr (!kPlain) if (kind[o] == 1 || kind[o] == 2) continue;
     if constexpr (kZero) if (kind[o] == 3) {
-      if (live) {
+      if (live && op.store_zero) {
         auto* dst = op.out_plane(grp, o, li) + kx;
         using OutT = typename std::remove_pointer<decltype(dst)>::type;
         const OutT z{};

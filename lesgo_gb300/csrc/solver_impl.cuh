@@ -1790,11 +1790,15 @@ class Solver : public SolverBase {
     post(tag, (double)g.nrows * ((double)in_fields * M * sizeof(R) + (double)NF * g.K * sizeof(T2)));
   }
 
+  // kz_even / kz_odd: modes kx from which the even / odd input fields are
+  // known to be zero (not read); -1: all K modes are read
   template <int NF, class Dst>
   void xinv(const Dst& dst, const T2* in, int M, int nyrows, int nli, const FftPlan<A>& plan, const char* tag = "xinv",
-            int out_fields = NF) {
+            int out_fields = NF, int kz_even = -1, int kz_odd = -1) {
     XiGeom g;
     g.M = M; g.K = d_.K; g.nyrows = nyrows; g.nrows = nyrows * nli * kp_.ninst; g.ls = M / 2 + 1;
+    g.kz0 = kz_even < 0 ? g.K : std::min(kz_even, g.K);
+    g.kz1 = kz_odd < 0 ? g.K : std::min(kz_odd, g.K);
     const int target = xtarget_;
     g.rpc = std::max(1, std::min(32, target / (NF * (M / 2))));
     g.in_field_stride = (long long)g.nrows * g.K;
@@ -1815,7 +1819,7 @@ class Solver : public SolverBase {
   template <int NIN, int NOUT, bool FWD, bool INV, typename InT, typename OutT>
   void ypass_lin(const InT* in, int in_lev0, int in_levstride, int in_inst_levels, int in_rows, OutT* out,
                  int out_rows, int nli, int ngroups, int rowmode, std::initializer_list<std::initializer_list<int>> mul,
-                 const char* tag = "ypass") {
+                 const char* tag = "ypass", bool store_zero_tiles = true) {
     const int nlev = nli * kp_.ninst;
     YOpLin<A, NIN, NOUT, InT, OutT> op;
     op.in = in;
@@ -1832,6 +1836,7 @@ class Solver : public SolverBase {
       ++o;
     }
     op.kxw = kxw_; op.kyw = kyw_; op.G1 = G1_; op.G2 = G2_;
+    op.store_zero = store_zero_tiles || !yshort_;
     for (int o = 0; o < NOUT; ++o) {
       // zero from the first column past its test filters' cutoffs (or never)
       int zf = -1;
@@ -1976,8 +1981,11 @@ class Solver : public SolverBase {
                        F_[LESGO_S22], F_[LESGO_S23], F_[LESGO_S33], d_.ld, d_.nz, kp_.lbc, kp_.ubc, kp_.plane,
                        imf(d_.nz)};
     xfwd<21>(src, d_.nx, d_.ny, d_.nz, specA_, px_, "lagrange.xfwd", 9);
+    // the 2-delta (even outputs) and 4-delta (odd) filtered spectra are zero
+    // past the filters' cutoff columns: the y pass does not write those
+    // tiles and the x inverse does not read those modes
     ypass_lin<1, 2, true, true, T2, T2>(specA_, 0, 1, d_.nz, d_.ny, specB_, d_.ny, d_.nz, 21, ROW_SAME,
-                                        {{MUL_G1}, {MUL_G2}}, "lagrange.ypass");
+                                        {{MUL_G1}, {MUL_G2}}, "lagrange.ypass", false);
     DstLagrange<R> dst;
     dst.FLMi = Ftmp_[0]; dst.FMMi = Ftmp_[1]; dst.FQNi = Ftmp_[2]; dst.FNNi = Ftmp_[3];
     dst.FLM = F_[LESGO_F_LM]; dst.FMM = F_[LESGO_F_MM]; dst.FQN = F_[LESGO_F_QN]; dst.FNN = F_[LESGO_F_NN];
@@ -1991,7 +1999,7 @@ class Solver : public SolverBase {
     dst.iflags = flags_d_;
     dst.plane = kp_.plane;
     dst.im = imf(d_.nz);
-    xinv<42>(dst, specB_, d_.nx, d_.ny, d_.nz, px_, "lagrange.xinv", 13);
+    xinv<42>(dst, specB_, d_.nx, d_.ny, d_.nz, px_, "lagrange.xinv", 13, kmax_g_[0] + 1, kmax_g_[1] + 1);
   }
 
   // convec.f90:21-333: vorticity and velocity to the 3/2 grid, the three

@@ -245,6 +245,7 @@ struct YOpLin {
   // and (inverse-only passes) the output it is i kx times (-1: none) with an
   // input whose multiplier in it is MUL_IKX
   int zero_from[NOUT];
+  bool store_zero = true;   // write the zero tiles (false: the consumer never reads those modes)
   bool sc_out[NOUT];
   int from[NOUT], from_in[NOUT];
 
