@@ -122,8 +122,8 @@ __global__ void __launch_bounds__(256) k_convec_rows(ConvRowsGeom g, FftPlan<R> 
         const T2 xk = k < g.K ? src[k] : czero<T2>();
         const int km = H - k;
         const T2 xm = (k > 0 && km < g.K) ? src[km] : czero<T2>();
-        const T2 a = mkc(xk.x + xm.x, xk.y - xm.y);
-        const T2 b = mkc(xk.x - xm.x, xk.y + xm.y);
+        const T2 a = cadd_conj(xk, xm);
+        const T2 b = csub_conj(xk, xm);
         const T2 w = ldt(plan.rtw + k);
         const R cx = w.x * b.x + w.y * b.y, cy = w.x * b.y - w.y * b.x;
         z = mkc(a.x - cy, a.y + cx);
@@ -209,8 +209,8 @@ __global__ void __launch_bounds__(256) k_convec_rows(ConvRowsGeom g, FftPlan<R> 
       if (r >= rows) continue;
       const T2 zk = Z[l * g.ls + kk];
       const T2 zm = Z[l * g.ls + (kk == 0 ? 0 : H - kk)];
-      const T2 a = mkc(zk.x + zm.x, zk.y - zm.y);
-      const T2 b = mkc(zk.x - zm.x, zk.y + zm.y);
+      const T2 a = cadd_conj(zk, zm);
+      const T2 b = csub_conj(zk, zm);
       const T2 w = ldt(plan.rtw + kk);
       const R wbx = w.x * b.x - w.y * b.y, wby = w.x * b.y + w.y * b.x;
       out[(long long)f * g.out_fs + (orow + row0 + r) * g.K + kk] = mkc(rmul_half(a.x + wby), rmul_half(a.y - wbx));

@@ -118,6 +118,15 @@ template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) {
 template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
   return __ffma2_rn(b, make_float2(-1.f, -1.f), a);   // a - b, exact product by -1
 }
+// a + conj(b) and a - conj(b) (the real-transform split steps)
+template <typename T2> __device__ __forceinline__ T2 cadd_conj(T2 a, T2 b) { return mkc(a.x + b.x, a.y - b.y); }
+template <typename T2> __device__ __forceinline__ T2 csub_conj(T2 a, T2 b) { return mkc(a.x - b.x, a.y + b.y); }
+template <> __device__ __forceinline__ float2 cadd_conj<float2>(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(1.f, -1.f), a);
+}
+template <> __device__ __forceinline__ float2 csub_conj<float2>(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, 1.f), a);
+}
 template <typename T2> __device__ __forceinline__ T2 cmulconj(T2 a, T2 b) {  // a * conj(b)
   return mkc(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
@@ -187,14 +196,26 @@ __device__ __forceinline__ void bfly4(T2& a0, T2& a1, T2& a2, T2& a3) {
   a3 = csub(t1, t3);
 }
 
+// a - b/2 and s*a (the radix-3 butterfly)
+template <typename T2> __device__ __forceinline__ T2 csub_half(T2 a, T2 b) {
+  return mkc(a.x - rmul_half(b.x), a.y - rmul_half(b.y));
+}
+template <> __device__ __forceinline__ float2 csub_half<float2>(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-0.5f, -0.5f), a);
+}
+template <typename T2, typename R> __device__ __forceinline__ T2 cscale(T2 a, R s) { return mkc(s * a.x, s * a.y); }
+template <> __device__ __forceinline__ float2 cscale<float2, float>(float2 a, float s) {
+  return __fmul2_rn(a, make_float2(s, s));
+}
+
 template <typename T2, bool INV>
 __device__ __forceinline__ void bfly3(T2& a0, T2& a1, T2& a2) {
   using R = decltype(a0.x);
   const R s = FftConst<R>::sin60();  // sin(2 pi / 3)
   T2 t1 = cadd(a1, a2);
-  T2 t2 = mkc(a0.x - rmul_half(t1.x), a0.y - rmul_half(t1.y));
+  T2 t2 = csub_half(a0, t1);
   T2 d = csub(a1, a2);
-  T2 t3 = mkc(s * d.x, s * d.y);
+  T2 t3 = cscale(d, s);
   a0 = cadd(a0, t1);
   // forward: y1 = t2 - i t3, y2 = t2 + i t3
   T2 it3 = mul_pi(t3);
@@ -370,8 +391,8 @@ __global__ void __launch_bounds__(256) k_xfwd(XfGeom g, FftPlan<R> plan, Src src
     if (row >= g.nrows) continue;
     T2 zk = Z[l * g.ls + kk];
     T2 zm = Z[l * g.ls + (kk == 0 ? 0 : H - kk)];
-    T2 a = mkc(zk.x + zm.x, zk.y - zm.y);   // Zk + conj(Zm)
-    T2 b = mkc(zk.x - zm.x, zk.y + zm.y);   // Zk - conj(Zm)
+    T2 a = cadd_conj(zk, zm);   // Zk + conj(Zm)
+    T2 b = csub_conj(zk, zm);   // Zk - conj(Zm)
     T2 w = ldt(plan.rtw + kk);
     // X = a/2 - (i/2) w b
     R wbx = w.x * b.x - w.y * b.y, wby = w.x * b.y + w.y * b.x;
@@ -416,8 +437,8 @@ __global__ void __launch_bounds__(256) k_xinv(XiGeom g, FftPlan<R> plan, const c
       T2 xk = k < kzf ? src[k] : czero<T2>();
       const int km = H - k;   // k = 0 -> Nyquist (zero)
       T2 xm = (k > 0 && km < kzf) ? src[km] : czero<T2>();
-      T2 a = mkc(xk.x + xm.x, xk.y - xm.y);
-      T2 b = mkc(xk.x - xm.x, xk.y + xm.y);
+      T2 a = cadd_conj(xk, xm);
+      T2 b = csub_conj(xk, xm);
       T2 w = ldt(plan.rtw + k);
       R cx = w.x * b.x + w.y * b.y, cy = w.x * b.y - w.y * b.x;  // conj(w) * b
       z = mkc(a.x - cy, a.y + cx);
