@@ -107,7 +107,9 @@ __global__ void __launch_bounds__(256) k_convec_rows(ConvRowsGeom g, FftPlan<R> 
     entry(e, lev, f0, nf);
     const bool ok = mbar_wait(bar, (unsigned)(e & 1));
     if (__syncthreads_or(!ok)) return false;
-    const FastDiv& fnl = nf == 6 ? g.f6 : nf == 3 ? g.f3 : g.f2;
+    // by value: a reference into the parameter block chosen at run time
+    // would make the compiler copy the block to local memory
+    const FastDiv fnl = nf == 6 ? g.f6 : nf == 3 ? g.f3 : g.f2;
     T2* X = base + (lev % 3) * slot_elems + (long long)f0 * rt * g.ls;
     T2* Sx = S + (long long)f0 * rt * g.ls;
     T2* A = (plan.nf & 1) ? Sx : X;

@@ -578,17 +578,22 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
   constexpr bool kZero = FWD && INV && NIN == 1;
   constexpr bool kDerive = !FWD && INV;
   constexpr bool kPlain = !SC && !kZero && !kDerive;   // every output takes the transforms
-  int kind[NOUT];
+  // two bits per output in a register (an array indexed in the output loop
+  // would live in local memory)
+  static_assert(NOUT <= 16, "two bits per output in 32");
+  unsigned kinds = 0;
+  auto kind = [&](int o) { return (int)((kinds >> (2 * o)) & 3u); };
   bool need_fwd = kPlain, any_sc = false;
   if constexpr (!kPlain) {
 #pragma unroll
     for (int o = 0; o < NOUT; ++o) {
-      kind[o] = 0;
-      if constexpr (kDerive) if (op.from[o] >= 0) kind[o] = 2;
-      if constexpr (kZero) if (kx0 >= op.zero_from[o]) kind[o] = 3;
-      if constexpr (SC) if (kind[o] == 0 && op.sc_out[o]) kind[o] = 1;
-      need_fwd |= kind[o] == 0;
-      any_sc |= kind[o] == 1;
+      int k = 0;
+      if constexpr (kDerive) if (op.from[o] >= 0) k = 2;
+      if constexpr (kZero) if (kx0 >= op.zero_from[o]) k = 3;
+      if constexpr (SC) if (k == 0 && op.sc_out[o]) k = 1;
+      kinds |= (unsigned)k << (2 * o);
+      need_fwd |= k == 0;
+      any_sc |= k == 1;
     }
   }
   if constexpr (SC) if (any_sc) {
@@ -621,7 +626,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
     }
     const R nyr = cvt<R>((double)g.ny_in);
     for (int o = 0; o < NOUT; ++o) {
-      if (kind[o] != 1) continue;
+      if (kind(o) != 1) continue;
       auto* dst = op.out_plane(grp, o, li) + kx;
       using OutT = typename std::remove_pointer<decltype(dst)>::type;
 #pragma unroll 2
@@ -643,8 +648,8 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
   }
   if (FWD && need_fwd) fft_cols<R, false>(L, L == S ? X : S, win, g.fwin, pin);   // ends in S
   for (int o = 0; o < NOUT; ++o) {
-    if constexpr (!kPlain) if (kind[o] == 1 || kind[o] == 2) continue;
-    if constexpr (kZero) if (kind[o] == 3) {
+    if constexpr (!kPlain) if (kind(o) == 1 || kind(o) == 2) continue;
+    if constexpr (kZero) if (kind(o) == 3) {
       if (live && op.store_zero) {
         auto* dst = op.out_plane(grp, o, li) + kx;
         using OutT = typename std::remove_pointer<decltype(dst)>::type;
@@ -681,7 +686,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
       // outputs that are i kx times this one (inverse passes: the transform
       // is linear and kx is constant on a column)
       if constexpr (kDerive) for (int o2 = o + 1; o2 < NOUT; ++o2) {
-        if (kind[o2] != 2 || op.from[o2] != o) continue;
+        if (kind(o2) != 2 || op.from[o2] != o) continue;
         T2 cf;
         op.coef(grp, o2, op.from_in[o2], kx, 0, cf);
         auto* d2 = op.out_plane(grp, o2, li) + kx;
