@@ -289,7 +289,7 @@ __device__ __forceinline__ void stage_bfly(const T2* src, T2* dst, int sr, int s
 
 template <typename T2, bool INV, int RR, bool FIRST>
 __device__ __forceinline__ void lines_stage(const T2* a, T2* b, int nl, int ls, int nb, int Ns,
-                                            const FastDiv& fnl, const FastDiv& fns, const T2* stw) {
+                                            const FastDiv fnl, const FastDiv fns, const T2* stw) {
   // the line index runs fastest across threads: with an odd line stride
   // the stage's loads and stores fall in distinct banks
   const int total = nl * nb;
@@ -309,7 +309,7 @@ template <typename T2> constexpr bool kRadix8 = !std::is_same<T2, dfc>::value;
 
 template <typename T2, bool INV, bool FIRST>
 __device__ __forceinline__ void lines_stage_r(int Rr, const T2* a, T2* b, int nl, int ls, int nb, int Ns,
-                                              const FastDiv& fnl, const FastDiv& fns, const T2* stw) {
+                                              const FastDiv fnl, const FastDiv fns, const T2* stw) {
   switch (Rr) {
     case 8:
       if constexpr (kRadix8<T2>) lines_stage<T2, INV, 8, FIRST>(a, b, nl, ls, nb, Ns, fnl, fns, stw);
@@ -323,8 +323,13 @@ __device__ __forceinline__ void lines_stage_r(int Rr, const T2* a, T2* b, int nl
 // Stockham autosort FFT of `nl` lines of length p.n held in shared memory
 // (line l at a + l*ls).  `b` is scratch of the same shape.  Returns the
 // buffer that holds the result.  All threads of the block must call it.
+//
+// The stage's sizes and divisors are read from the plan once per stage and
+// passed by value (registers): the plan lives in the kernel's parameter
+// block, and a reference into it with the run-time stage index would be
+// re-read through the constant path inside the butterfly loop.
 template <typename R, bool INV>
-__device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FastDiv& fnl, const FftPlan<R>& p) {
+__device__ cplx<R>* fft_lines(cplx<R>* a, cplx<R>* b, int nl, int ls, const FastDiv fnl, const FftPlan<R>& p) {
   for (int s = 0; s < p.nf; ++s) {
     const int nb = p.nbs[s], Ns = p.nss[s];
     if (s == 0)
@@ -477,8 +482,8 @@ struct YGeom {
 };
 
 template <typename T2, bool INV, int RR, bool FIRST>
-__device__ __forceinline__ void cols_stage(const T2* a, T2* b, int width, const FastDiv& fw, int nb, int Ns,
-                                           const FastDiv& fns, const T2* stw) {
+__device__ __forceinline__ void cols_stage(const T2* a, T2* b, int width, const FastDiv fw, int nb, int Ns,
+                                           const FastDiv fns, const T2* stw) {
   const int total = nb * width;
   const int sr = nb * width, sd = Ns * width;   // strides between a butterfly's inputs / outputs
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
@@ -492,8 +497,8 @@ __device__ __forceinline__ void cols_stage(const T2* a, T2* b, int width, const 
 }
 
 template <typename T2, bool INV, bool FIRST>
-__device__ __forceinline__ void cols_stage_r(int Rr, const T2* a, T2* b, int width, const FastDiv& fw, int nb, int Ns,
-                                             const FastDiv& fns, const T2* stw) {
+__device__ __forceinline__ void cols_stage_r(int Rr, const T2* a, T2* b, int width, const FastDiv fw, int nb, int Ns,
+                                             const FastDiv fns, const T2* stw) {
   switch (Rr) {
     case 8:
       if constexpr (kRadix8<T2>) cols_stage<T2, INV, 8, FIRST>(a, b, width, fw, nb, Ns, fns, stw);
@@ -509,7 +514,7 @@ __device__ __forceinline__ void cols_stage_r(int Rr, const T2* a, T2* b, int wid
 // the column fastest, so a warp touches consecutive addresses at every step
 // (no bank conflicts); the butterflies are those of fft_lines.
 template <typename R, bool INV>
-__device__ cplx<R>* fft_cols(cplx<R>* a, cplx<R>* b, int width, const FastDiv& fw, const FftPlan<R>& p) {
+__device__ cplx<R>* fft_cols(cplx<R>* a, cplx<R>* b, int width, const FastDiv fw, const FftPlan<R>& p) {
   for (int s = 0; s < p.nf; ++s) {
     const int nb = p.nbs[s], Ns = p.nss[s];
     if (s == 0)
