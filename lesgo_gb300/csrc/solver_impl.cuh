@@ -2180,8 +2180,12 @@ class Solver : public SolverBase {
     const long long ncol = pl_s * kp_.ninst;
     const int nu = nz + 1;
     const bool seq = thomas_mode_ == 1 || (thomas_mode_ == 0 && ncol >= 12288);
+    // four levels per register chunk: 96 registers a thread (164 with
+    // eight), so the sweep leaves room on the SMs for the other handles'
+    // kernels running beside it (the ensemble step measured 1 % shorter;
+    // the sweep alone takes the same time)
     if (seq)
-      k_thomas_seq<8><<<(unsigned)((ncol + 127) / 128), 128, 0, st_>>>(ta);
+      k_thomas_seq<4><<<(unsigned)((ncol + 127) / 128), 128, 0, st_>>>(ta);
     else if (nu <= 192)
       k_thomas_r<16, 8, 12><<<(unsigned)((ncol + 7) / 8), 128, 0, st_>>>(ta);
     else
