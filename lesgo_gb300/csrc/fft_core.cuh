@@ -670,6 +670,7 @@ __global__ void __launch_bounds__(256) k_ypass(YGeom g, FftPlan<R> pin, FftPlan<
       if (live && kin >= 0) {
 #pragma unroll
         for (int i = 0; i < NIN; ++i) {
+          if (NIN > 1 && op.is_zero(o, i)) continue;   // inputs this output does not use
           T2 cf;
           const T2 v = S[kin * win + i * g.tk + c];
           if (op.is_one(o, i)) acc = cadd(acc, v);

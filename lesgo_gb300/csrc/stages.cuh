@@ -273,6 +273,7 @@ struct YOpLin {
   }
   // a plain copy of input i into output o (no multiply)
   __device__ __forceinline__ bool is_one(int o, int i) const { return mul[o][i] == MUL_ONE; }
+  __device__ __forceinline__ bool is_zero(int o, int i) const { return mul[o][i] == MUL_ZERO; }
   __device__ __forceinline__ bool same_rows() const { return rowmode == ROW_SAME; }
 
   __device__ __forceinline__ bool coef(int g, int o, int i, int kx, int kin, cplx<R>& cf) const {
